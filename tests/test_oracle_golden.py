@@ -1,0 +1,79 @@
+"""The oracle against golden vectors produced by the reference's own source.
+
+The fixtures in tests/golden/ come from executing Process/{CG,BiCG,CGS,
+Prec1,Resid}.f90 statement by statement (tests/golden/make_golden.py); the C
+restatement in oracle/ must reproduce every output bit for bit, including
+the module state carried between calls and the early-exit and
+non-convergence conventions.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+SOLVER_CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                      if not os.path.basename(p).startswith("prec1_resid"))
+PR_CASES = sorted(glob.glob(os.path.join(GOLDEN, "prec1_resid_*.npz")))
+
+
+def _same(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64) if a.dtype == np.float64
+                                                 else a, b.view(np.uint64)
+                                                 if b.dtype == np.float64 else b)
+
+
+def test_fixture_inventory():
+    assert len(SOLVER_CASES) >= 20 and len(PR_CASES) == 2
+
+
+@pytest.mark.parametrize("path", SOLVER_CASES, ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_reproduces_reference_solver(path):
+    g = np.load(path)
+    oracle.reset_state()
+    for c in range(int(g["ncalls"])):
+        p = f"c{c}_"
+        x, r, it, ini, fin = oracle.solve(
+            str(g[p + "method"]), int(g["N"]), int(g["NB"]), int(g["NONZ"]), g["A"], g["Acol"],
+            g["Arow"], g["Adia"], g["Ab"], g[p + "x_in"], g[p + "r1_in"], int(g[p + "prec"]),
+            int(g[p + "niter_in"]), float(g[p + "tol"]), float(g[p + "IniRes_in"]),
+            float(g[p + "FinRes_in"]))
+        assert it == int(g[p + "niter_out"])
+        assert _same(x, g[p + "x_out"]), "x differs"
+        assert _same(r, g[p + "r1_out"]), "r1 differs"
+        assert _same(np.float64(ini), g[p + "IniRes_out"])
+        assert _same(np.float64(fin), g[p + "FinRes_out"])
+        assert _same(np.float64(oracle.error_state()), g[p + "error_state"])
+
+
+@pytest.mark.parametrize("path", PR_CASES, ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_reproduces_reference_prec1_resid(path):
+    g = np.load(path)
+    for prec in (0, 1, 2):
+        D = oracle.prec1(int(g["N"]), int(g["NONZ"]), g["A"], g["Acol"], g["Arow"], g["Adia"],
+                         prec)
+        assert _same(D, g[f"D_prec{prec}"])
+    r = oracle.resid(int(g["N"]), int(g["NB"]), int(g["NONZ"]), g["A"], g["Acol"], g["Arow"],
+                     g["Ab"], g["resid_x"], g["resid_r1_in"])
+    assert _same(r, g["resid_r1_out"])
+
+
+def test_bicg_iterates_equal_cg_bitwise():
+    """The reference's BiCG multiplies its shadow sequence by A (not A^T)
+    and starts it at r1, so it reproduces CG's outputs exactly
+    (Process/BiCG.f90:93-95,193-212)."""
+    for path in SOLVER_CASES:
+        g = np.load(path)
+        if int(g["ncalls"]) != 1 or str(g["c0_method"]) not in ("cg", "bicg"):
+            continue
+        args = (int(g["N"]), int(g["NB"]), int(g["NONZ"]), g["A"], g["Acol"], g["Arow"],
+                g["Adia"], g["Ab"], g["c0_x_in"], g["c0_r1_in"], int(g["c0_prec"]),
+                int(g["c0_niter_in"]), float(g["c0_tol"]))
+        a = oracle.solve("cg", *args)
+        b = oracle.solve("bicg", *args)
+        assert a[2] == b[2]
+        assert _same(a[0], b[0]) and _same(a[1], b[1])
