@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Krylov solver core.
+
+Metric: time to a 1e-8 relative residual of the T-FlowS solvers, reported as
+whole-job solves/s (higher is better), with the HBM bandwidth the solver
+kernel achieves.  Default workload: 128^3 perturbed-hex convection-diffusion
+system (momentum / scalar transport), BiCG with diagonal preconditioning in
+FP64 (the reference's arithmetic and convergence test, absolute tolerance
+1e-8*||b||), x0 = 0.  Synthetic data (seeded); the matrix and vectors
+(~260 MB) exceed the 129 MB L2, so no flush is needed between steps.
+
+A "step" is one complete solve.  `value` times K solves on data resident in
+HBM (device API); `e2e` times K calls of the Fortran-facing C ABI
+(tflows_bicg) with the matrix, x and b in pinned host memory, host<->device
+copies inside each call.  The CPU baseline is the oracle (the reference's
+algorithm restated in C) on the host cores.
+
+Multi-GPU: the solves are independent replicas (one per rank, no
+collective); value = total solves / max-over-ranks time.
+
+--impl reference: the reference algorithm (oracle port, FP64, serial per
+solve as in the reference) on the host cores, one solve per core at a time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CG/BiCG time-to-1e-8 residual & HBM GB/s: mixed-prec vs FP64, 1 GB300"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [v.strip() for v in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax = float(f[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        finally:
+            os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference_throughput(s, method, prec, threads, seconds_budget):
+    """Oracle solves of the same system on `threads` host threads, one solve
+    per thread at a time, for about `seconds_budget`; returns (solves/s,
+    solves done, iterations)."""
+    import oracle
+    oracle.build()
+    done = [0] * threads
+    its = [0]
+    stop = time.perf_counter() + seconds_budget
+
+    def work(t):
+        while True:
+            _, _, it, _, _ = oracle.solve(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia,
+                                          s.Ab, s.x, s.b, prec, 200, s.tol)
+            its[0] = it
+            done[t] += 1
+            if time.perf_counter() >= stop:
+                break
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work, args=(t,)) for t in range(threads)]
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    el = time.perf_counter() - t0
+    return sum(done) / el, sum(done), its[0], el
+
+
+def run_reference(args):
+    import __graft_entry__ as ge
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    pkg = ge.load_package()
+    s = pkg.mesh.config_system(2)
+    cores = os.cpu_count() or 1
+    # W warm-up steps and K timed steps; each step is one round of
+    # concurrent solves (one per core).
+    import oracle
+    oracle.build()
+    for _ in range(args.warmup):
+        cpu_reference_throughput(s, "bicg", 1, cores, 0.0)
+    t0 = time.perf_counter()
+    total = 0
+    it = 0
+    for _ in range(args.steps):
+        _, n, it, _ = cpu_reference_throughput(s, "bicg", 1, cores, 0.0)
+        total += n
+    el = time.perf_counter() - t0
+    value = total / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(s, "bicg", 1),
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} concurrent full BiCG solves per step "
+                                   f"({it} iterations each), oracle C restatement, 1 thread each"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(s, method, prec):
+    return {"workload": "cfg2 convection-diffusion 128^3 perturbed hex, BiCG + diagonal, FP64, "
+                        "tol 1e-8*||b|| (absolute, reference test), x0=0",
+            "n": s.N, "nnz": s.nnz, "method": method, "prec": prec,
+            "l2": "inputs larger than L2 (no flush)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import __graft_entry__ as ge
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    pkg = ge.load_package()
+    pkg.load_library()
+    peak, peak_kind = load_peaks()
+
+    s = pkg.mesh.config_system(2)
+    method, prec = "bicg", 1
+    tol = s.tol
+    dev = torch.device("cuda", local)
+    topo = pkg.Topology.from_system(s)
+    val = torch.from_numpy(s.A[:-1].copy()).to(dev)
+    b = torch.from_numpy(s.b.copy()).to(dev)
+    x = torch.zeros(s.N, dtype=torch.float64, device=dev)
+
+    def step():
+        x.zero_()
+        return topo.solve(val, b, x, method, prec, 200, tol)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        res = step()
+    if res["status"] != pkg.OK:
+        raise RuntimeError(f"solve failed: {res}")
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kern_s, kern_b, iters = 0.0, 0.0, []
+    e0.record()
+    for _ in range(args.steps):
+        r = step()
+        kern_s += r["seconds"]
+        kern_b += r["bytes"]
+        iters.append(r["iterations"])
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    el = e0.elapsed_time(e1) * 1e-3
+    if world > 1:
+        t = torch.tensor([el], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el = float(t.item())
+    value = world * args.steps / el
+
+    # e2e through the Fortran-facing C ABI, inputs in pinned host memory.
+    A_h = torch.from_numpy(s.A.copy()).pin_memory().numpy()
+    x_h = torch.zeros(s.NB + s.N + 1, dtype=torch.float64).pin_memory().numpy()
+    r_h = torch.zeros(s.N, dtype=torch.float64).pin_memory().numpy()
+    pkg.set_options()
+    e2e_t = 0.0
+    for k in range(args.warmup + args.steps):
+        x_h[:] = 0.0
+        r_h[:] = s.b
+        t0 = time.perf_counter()
+        out = pkg.bicg(s.N, s.NB, s.NONZ, A_h, s.Acol, s.Arow, s.Adia, s.Ab, x_h, r_h, prec, 200,
+                       tol)
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_t += t1 - t0
+    if out.status != pkg.OK:
+        raise RuntimeError(f"e2e solve failed: {out}")
+    if world > 1:
+        t = torch.tensor([e2e_t], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e = world * args.steps / e2e_t
+
+    # standalone SELL products (FP64 and FP32) for the SpMV roofline
+    y = torch.empty_like(x)
+    xs = torch.rand(s.N, dtype=torch.float64, device=dev)
+    spmv64 = topo.spmv(val, xs, y, repeat=20)
+    sl = (s.N + 31) // 32
+    b64 = s.nnz * 12.0 + 8.0 * (sl + 1) + 16.0 * s.N
+
+    achieved = kern_b / kern_s / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(s, method, prec),
+        "iterations": int(statistics.median(iters)),
+        "time_to_tol_ms": 1e3 * el / args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "krylov_kernel<double> (persistent BiCG/CG solve)",
+                     "peak_kind": peak_kind},
+        "spmv_fp64": {"gbs": b64 / spmv64 / 1e9, "frac": b64 / spmv64 / 1e9 / peak,
+                      "ms": spmv64 * 1e3},
+        "e2e": {"value": e2e, "unit": "solves/s",
+                "h2d_bytes_per_step": int(8 * s.nnz + 16 * s.N),
+                "d2h_bytes_per_step": int(16 * s.N)},
+        "clocks": clk,
+        "gpu_launches": 2 * args.steps,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, n, it, el_c = cpu_reference_throughput(s, method, prec, 1, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
+                                "sample": f"{n} full BiCG solves ({it} iterations) of the same "
+                                          f"system, oracle C restatement, 1 thread, {el_c:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,182 @@
+/*
+ * tflows_krylov.h -- C ABI of libtflows_krylov.so, the GB300 (sm_103a)
+ * Krylov linear-solver core that replaces the T-FlowS solver subroutines.
+ *
+ * Legacy entry points keep the Fortran subroutine interfaces unchanged: all
+ * arguments by reference, 1-based compressed-row arrays exactly as
+ * Process/TopolM.f90 builds them (Acol = row pointers N+1, Arow = column
+ * indices, Adia = diagonal positions, NONZ = stored entries + 1), x passed at
+ * x(-NB) and Ab at Ab(-NB).  They mirror the reference outputs: x, r1 (the
+ * final recursive residual), niter (iterations used, or niter_in+1 when the
+ * tolerance was not reached), IniRes, FinRes.  Nothing here aborts the
+ * calling process; tflows_last_status() reports what happened.
+ *
+ * Every call is synchronous and returns after x and r1 are back in host
+ * memory.  The library keeps a per-device context (stream, workspace and a
+ * cache of device copies of the matrix topology keyed by its pointers, sizes
+ * and a sampled content hash); tflows_finalize() releases it.
+ */
+#ifndef TFLOWS_KRYLOV_H
+#define TFLOWS_KRYLOV_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TFLOWS_OK             0 /* tolerance reached (or an early exit)    */
+#define TFLOWS_NOT_CONVERGED  1 /* iteration limit reached                 */
+#define TFLOWS_BREAKDOWN      2 /* (p,Ap) or rho vanished (mixed mode)      */
+#define TFLOWS_NONFINITE      3 /* residual norm became Inf/NaN            */
+#define TFLOWS_TIMEOUT        4 /* a device-side wait exceeded its limit   */
+#define TFLOWS_BAD_INPUT      5 /* rejected on the host before any launch  */
+#define TFLOWS_CUDA_ERROR     6 /* a CUDA runtime call failed              */
+#define TFLOWS_NO_DEVICE      7 /* no CUDA device available                */
+#define TFLOWS_UNSUPPORTED    8 /* option combination not implemented      */
+
+/* ---- methods, precisions, tolerance modes -------------------------------- */
+#define TFLOWS_METHOD_CG        0 /* Process/CG.f90                          */
+#define TFLOWS_METHOD_BICG      1 /* Process/BiCG.f90 (shadow uses A)        */
+#define TFLOWS_METHOD_CGS       2 /* Process/CGS.f90                         */
+#define TFLOWS_METHOD_BICG_TRUE 3 /* extension: shadow sequence uses A^T     */
+
+#define TFLOWS_FP64  0 /* reference arithmetic: FP64 throughout              */
+#define TFLOWS_MIXED 1 /* FP32 inner Krylov solves inside FP64 refinement    */
+
+#define TFLOWS_TOL_ABSOLUTE 0 /* stop when ||r||_2 < tol (the reference)    */
+#define TFLOWS_TOL_RELATIVE 1 /* stop when ||r||_2 < tol * ||b||_2           */
+
+typedef struct tflows_options {
+    int precision;       /* TFLOWS_FP64 (default) or TFLOWS_MIXED            */
+    int tol_mode;        /* TFLOWS_TOL_ABSOLUTE (default) or _RELATIVE       */
+    double inner_rtol;   /* mixed: inner residual reduction per refinement   */
+    int inner_maxiter;   /* mixed: inner iteration cap per refinement        */
+    int max_refinements; /* mixed: outer FP64 refinement steps cap          */
+    int ic_sweeps;       /* mixed + prec 2: 0 = exact triangular sweeps,
+                            k > 0 = k Jacobi sweeps per triangle            */
+    int ic_bf16;         /* mixed + prec 2: IC off-diagonals stored in BF16 */
+    double timeout_s;    /* limit for any single device-side wait           */
+    int block_size;      /* threads per block, 0 = tuned                     */
+    int grid_blocks;     /* persistent blocks, 0 = tuned                     */
+    int device;          /* CUDA device ordinal, -1 = current                */
+} tflows_options;
+
+typedef struct tflows_result {
+    int status;           /* TFLOWS_* status code                           */
+    int iterations;       /* reference-visible iteration count              */
+    int inner_iterations; /* mixed: total inner iterations                  */
+    int refinements;      /* mixed: FP64 refinement steps                   */
+    double ini_res;       /* ||b - A x0||_2                                 */
+    double fin_res;       /* final recursive (FP64) or true (mixed) norm    */
+    double seconds;       /* device time of the solve kernels               */
+    double bytes;         /* algorithmic bytes moved by the solve kernels   */
+} tflows_result;
+
+/* Fill *opt with the defaults (reference arithmetic and tolerance). */
+void tflows_default_options(tflows_options *opt);
+/* Options used by the legacy entry points below (copied). */
+int tflows_set_options(const tflows_options *opt);
+
+/* ---- legacy Fortran-facing entry points ---------------------------------- */
+/* Replaces SUBROUTINE cg (Process/CG.f90:2-34). */
+void tflows_cg(const int *N, const int *NB, const int *NONZ, const double *A,
+               const int *Acol, const int *Arow, const int *Adia,
+               const double *Ab, double *x, double *r1, const int *prec,
+               int *niter, const double *tol, double *IniRes, double *FinRes);
+/* Replaces SUBROUTINE bicg (Process/BiCG.f90:2-34). */
+void tflows_bicg(const int *N, const int *NB, const int *NONZ, const double *A,
+                 const int *Acol, const int *Arow, const int *Adia,
+                 const double *Ab, double *x, double *r1, const int *prec,
+                 int *niter, const double *tol, double *IniRes,
+                 double *FinRes);
+/* Replaces SUBROUTINE CGS (Process/CGS.f90:2-34). */
+void tflows_cgs(const int *N, const int *NB, const int *NONZ, const double *A,
+                const int *Acol, const int *Arow, const int *Adia,
+                const double *Ab, double *x, double *r1, const int *prec,
+                int *niter, const double *tol, double *IniRes, double *FinRes);
+/* Replaces SUBROUTINE Prec1 (Process/Prec1.f90:2-18): D <- diag | IC(0)
+ * inverse pivots | 1 for prec = 1 | 2 | other. */
+void tflows_prec1(const int *N, const int *NONZ, const double *A,
+                  const int *Acol, const int *Arow, const int *Adia,
+                  double *D, const int *prec);
+/* Replaces SUBROUTINE Resid (Process/Resid.f90:2-16): r1 <- r1 - A x. */
+void tflows_resid(const int *N, const int *NB, const int *NONZ,
+                  const double *A, const int *Acol, const int *Arow,
+                  const double *Ab, const double *x, double *r1);
+
+/* Status of the last call made on this thread, and a readable message. */
+int tflows_last_status(void);
+const char *tflows_status_string(int status);
+const char *tflows_last_error(void);
+/* Result details of the last solve made on this thread. */
+void tflows_last_result(tflows_result *res);
+/* Release every device resource the library holds. */
+void tflows_finalize(void);
+
+/* ---- extended host-pointer entry point ------------------------------------ */
+/* Same arguments and outputs as tflows_cg/bicg/cgs plus a method, options
+ * (NULL = the legacy options) and a result record (may be NULL).  Returns
+ * the status code. */
+int tflows_solve_ex(int method, const int *N, const int *NB, const int *NONZ,
+                    const double *A, const int *Acol, const int *Arow,
+                    const int *Adia, const double *Ab, double *x, double *r1,
+                    const int *prec, int *niter, const double *tol,
+                    double *IniRes, double *FinRes,
+                    const tflows_options *opt, tflows_result *res);
+
+/* ---- device-pointer interface (used by the PyTorch binding) -------------- */
+typedef struct tflows_topology tflows_topology;
+
+/* Register a compressed-row pattern.  rowptr (n+1), col (nnz), diag (n) use
+ * `index_base` (0 or 1); they are device pointers when `on_device` is 1 and
+ * host pointers otherwise.  The library copies what it needs. */
+int tflows_topology_create(tflows_topology **out, int n, int nnz,
+                           const int *rowptr, const int *col, const int *diag,
+                           int index_base, int on_device);
+void tflows_topology_destroy(tflows_topology *topo);
+/* Positions of the transposed entries: tpos[k] = stored position of (j,i)
+ * for the entry k at (i,j); -1 where the pattern has no such entry.
+ * Device int array of nnz elements, valid while the topology lives. */
+const int *tflows_topology_transpose_map(tflows_topology *topo);
+
+/* Solve A x = b with device arrays in the topology's stored order: val
+ * (nnz FP64), b (n), x (n, in/out: initial guess and solution), r_out (n,
+ * may be NULL: final recursive residual).  `stream` is a cudaStream_t (NULL
+ * = the library's own).  Synchronous: returns when the result is final. */
+int tflows_solve_device(tflows_topology *topo, int method, int prec,
+                        const tflows_options *opt, const double *val,
+                        const double *b, double *x, double *r_out,
+                        int maxiter, double tol, void *stream,
+                        tflows_result *res);
+
+/* Batched solve: `count` independent systems, each with its own topology,
+ * method and preconditioner, run by one persistent launch.  Arrays of
+ * per-system device pointers as in tflows_solve_device. */
+int tflows_solve_batched_device(int count, tflows_topology *const *topos,
+                                const int *methods, const int *precs,
+                                const tflows_options *opt,
+                                const double *const *vals,
+                                const double *const *bs, double *const *xs,
+                                const int *maxiters, const double *tols,
+                                void *stream, tflows_result *results);
+
+/* grad_val[k] = -lambda[row(k)] * x[col(k)] over the stored pattern: the
+ * gradient of a scalar loss with respect to the matrix entries, given the
+ * adjoint solution lambda (A^T lambda = dL/dx) and the solution x. */
+int tflows_pattern_outer(tflows_topology *topo, const double *lambda,
+                         const double *x, double *grad_val, void *stream);
+
+/* Standalone compressed-row product y = A x on device arrays (FP64 or, with
+ * fp32 = 1, values/vectors converted to FP32 on the fly).  For tests and
+ * bandwidth measurement; returns the kernel time in seconds through *sec. */
+int tflows_spmv_device(tflows_topology *topo, const double *val,
+                       const double *x, double *y, int repeat, int fp32,
+                       void *stream, double *sec);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TFLOWS_KRYLOV_H */

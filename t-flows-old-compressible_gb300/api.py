@@ -1,0 +1,278 @@
+"""Python mirror of the reference's solver interface over the C ABI.
+
+``cg``, ``bicg``, ``cgs``, ``prec1`` and ``resid`` take the same arguments
+as the Fortran subroutines (Process/CG.f90:2-34, BiCG.f90, CGS.f90,
+Prec1.f90:2-18, Resid.f90:2-16) as numpy arrays in the same layout: 1-based
+``Acol``/``Arow``/``Adia``, ``x`` holding x(-NB:N), ``Ab`` holding
+Ab(-NB:-1).  Like the Fortran dummies, ``x`` and ``r1`` (and ``D``) are
+updated in place; the scalar outputs (niter, IniRes, FinRes) are returned.
+Every call goes through libtflows_krylov.so on the GPU; there is no CPU path.
+
+``Topology`` is the device-array interface used by the PyTorch binding: a
+registered compressed-row pattern whose solves take torch CUDA tensors and
+run on torch's current stream.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import NamedTuple
+
+import numpy as np
+
+from . import _native
+
+OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT, BAD_INPUT, CUDA_ERROR, NO_DEVICE, UNSUPPORTED = \
+    range(9)
+CG, BICG, CGS, BICG_TRUE = 0, 1, 2, 3
+FP64, MIXED = 0, 1
+TOL_ABSOLUTE, TOL_RELATIVE = 0, 1
+METHODS = {"cg": CG, "bicg": BICG, "cgs": CGS, "bicg_true": BICG_TRUE}
+
+
+class SolverError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{status_string(status)}: {message}")
+        self.status = status
+
+
+class SolveOutput(NamedTuple):
+    niter: int
+    IniRes: float
+    FinRes: float
+    status: int
+
+
+def lib():
+    return _native.load()
+
+
+def status_string(st: int) -> str:
+    return lib().tflows_status_string(int(st)).decode()
+
+
+def last_status() -> int:
+    return lib().tflows_last_status()
+
+
+def last_error() -> str:
+    return lib().tflows_last_error().decode()
+
+
+def last_result() -> dict:
+    r = _native.Result()
+    lib().tflows_last_result(ctypes.byref(r))
+    return r.as_dict()
+
+
+def options(**kw) -> _native.Options:
+    o = _native.Options()
+    lib().tflows_default_options(ctypes.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def set_options(**kw) -> None:
+    lib().tflows_set_options(ctypes.byref(options(**kw)))
+
+
+def finalize() -> None:
+    lib().tflows_finalize()
+
+
+def _ci(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _cd(a, writable=False):
+    if writable:
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+            raise TypeError("in/out arrays must be C-contiguous float64 numpy arrays")
+    else:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _byref_i(v):
+    return ctypes.c_int(int(v))
+
+
+def solve_ex(method, N, NB, NONZ, A, Acol, Arow, Adia, Ab, x, r1, prec, niter, tol,
+             IniRes=0.0, FinRes=0.0, opts=None, raise_on_error=True):
+    """tflows_solve_ex: one of the reference solvers with options.  ``x``
+    (length NB+N+1) and ``r1`` (length N) are updated in place."""
+    m = METHODS.get(method, method)
+    A_, pA = _cd(A)
+    Acol_, pAcol = _ci(Acol)
+    Arow_, pArow = _ci(Arow)
+    Adia_, pAdia = _ci(Adia)
+    Ab_, pAb = _cd(Ab if NB > 0 else np.zeros(1))
+    _, px = _cd(x, writable=True)
+    _, pr = _cd(r1, writable=True)
+    cN, cNB, cNZ, cp, cit = (_byref_i(N), _byref_i(NB), _byref_i(NONZ), _byref_i(prec),
+                             _byref_i(niter))
+    ctol, cini, cfin = ctypes.c_double(tol), ctypes.c_double(IniRes), ctypes.c_double(FinRes)
+    res = _native.Result()
+    st = lib().tflows_solve_ex(int(m), ctypes.byref(cN), ctypes.byref(cNB), ctypes.byref(cNZ),
+                               pA, pAcol, pArow, pAdia, pAb, px, pr, ctypes.byref(cp),
+                               ctypes.byref(cit), ctypes.byref(ctol), ctypes.byref(cini),
+                               ctypes.byref(cfin), ctypes.byref(opts) if opts else None,
+                               ctypes.byref(res))
+    if raise_on_error and st in (BAD_INPUT, CUDA_ERROR, NO_DEVICE, UNSUPPORTED, TIMEOUT):
+        raise SolverError(st, last_error())
+    return SolveOutput(cit.value, cini.value, cfin.value, st)
+
+
+def _legacy(method):
+    def fn(N, NB, NONZ, A, Acol, Arow, Adia, Ab, x, r1, prec, niter, tol, IniRes=0.0,
+           FinRes=0.0):
+        return solve_ex(method, N, NB, NONZ, A, Acol, Arow, Adia, Ab, x, r1, prec, niter, tol,
+                        IniRes, FinRes, opts=None)
+    fn.__name__ = method
+    fn.__doc__ = (f"The reference's `{method}` (Process/{ {'cg': 'CG', 'bicg': 'BiCG', 'cgs': 'CGS'}[method]}.f90) "
+                  "on the GPU: x and r1 updated in place; returns (niter, IniRes, FinRes, status).")
+    return fn
+
+
+cg = _legacy("cg")
+bicg = _legacy("bicg")
+cgs = _legacy("cgs")
+
+
+def prec1(N, NONZ, A, Acol, Arow, Adia, D, prec):
+    """Process/Prec1.f90: fills D (length N, float64) in place."""
+    _, pA = _cd(A)
+    _, pAcol = _ci(Acol)
+    _, pArow = _ci(Arow)
+    _, pAdia = _ci(Adia)
+    _, pD = _cd(D, writable=True)
+    lib().tflows_prec1(ctypes.byref(_byref_i(N)), ctypes.byref(_byref_i(NONZ)), pA, pAcol,
+                       pArow, pAdia, pD, ctypes.byref(_byref_i(prec)))
+    st = last_status()
+    if st != OK:
+        raise SolverError(st, last_error())
+
+
+def resid(N, NB, NONZ, A, Acol, Arow, Ab, x, r1):
+    """Process/Resid.f90: r1 <- r1 - A x, r1 updated in place."""
+    _, pA = _cd(A)
+    _, pAcol = _ci(Acol)
+    _, pArow = _ci(Arow)
+    _, pAb = _cd(Ab if NB > 0 else np.zeros(1))
+    _, px = _cd(x)
+    _, pr = _cd(r1, writable=True)
+    lib().tflows_resid(ctypes.byref(_byref_i(N)), ctypes.byref(_byref_i(NB)),
+                       ctypes.byref(_byref_i(NONZ)), pA, pAcol, pArow, pAb, px, pr)
+    st = last_status()
+    if st != OK:
+        raise SolverError(st, last_error())
+
+
+def solve_system(method, s, prec, niter=1000, tol=None, x=None, b=None, opts=None):
+    """Convenience: solve a mesh.System; returns (x(-NB:N), r1, SolveOutput, result dict)."""
+    xo = (s.x if x is None else x).astype(np.float64, copy=True)
+    ro = (s.b if b is None else b).astype(np.float64, copy=True)
+    out = solve_ex(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab, xo, ro, prec,
+                   niter, s.tol if tol is None else tol, opts=opts)
+    return xo, ro, out, last_result()
+
+
+# ---- device-array interface -------------------------------------------------------
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Topology:
+    """A compressed-row pattern registered on the current CUDA device.
+
+    ``rowptr``, ``col``, ``diag`` are int32 arrays (numpy or torch, host or
+    CUDA) with the given index base.  Solves take torch CUDA tensors.
+    """
+
+    def __init__(self, n, rowptr, col, diag, index_base=0):
+        import torch
+        self.n = int(n)
+        self.nnz = int(len(col))
+        self._h = ctypes.c_void_p()
+        on_dev = 0
+        keep = []
+        arrs = []
+        for a in (rowptr, col, diag):
+            if isinstance(a, torch.Tensor):
+                a = a.to(torch.int32).contiguous()
+                on_dev = 1 if a.is_cuda else on_dev
+                keep.append(a)
+                arrs.append(ctypes.c_void_p(a.data_ptr()))
+            else:
+                a = np.ascontiguousarray(a, dtype=np.int32)
+                keep.append(a)
+                arrs.append(ctypes.c_void_p(a.ctypes.data))
+        st = lib().tflows_topology_create(ctypes.byref(self._h), self.n, self.nnz, *arrs,
+                                          int(index_base), on_dev)
+        if st != OK:
+            raise SolverError(st, last_error())
+
+    @classmethod
+    def from_system(cls, s):
+        return cls(s.N, s.Acol, s.Arow[:-1], s.Adia, index_base=1)
+
+    def close(self):
+        if self._h:
+            lib().tflows_topology_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def transpose_map(self):
+        """Device pointer of the transposed-entry map (int32, nnz)."""
+        p = lib().tflows_topology_transpose_map(self._h)
+        if not p:
+            raise SolverError(CUDA_ERROR, last_error())
+        return p
+
+    def solve(self, val, b, x, method="cg", prec=1, maxiter=1000, tol=1e-8, r_out=None,
+              opts=None, raise_on_error=True):
+        """Solve in place on torch CUDA float64 tensors (x: initial guess in,
+        solution out).  Returns the result record as a dict."""
+        for t in (val, b, x):
+            if not (t.is_cuda and t.dtype.itemsize == 8 and t.is_contiguous()):
+                raise TypeError("val, b, x must be contiguous CUDA float64 tensors")
+        res = _native.Result()
+        st = lib().tflows_solve_device(self._h, int(METHODS.get(method, method)), int(prec),
+                                       ctypes.byref(opts) if opts else None, _ptr(val), _ptr(b),
+                                       _ptr(x), _ptr(r_out) if r_out is not None else None,
+                                       int(maxiter), float(tol), _stream(), ctypes.byref(res))
+        if raise_on_error and st in (BAD_INPUT, CUDA_ERROR, NO_DEVICE, UNSUPPORTED, TIMEOUT):
+            raise SolverError(st, last_error())
+        return res.as_dict()
+
+    def spmv(self, val, x, y, repeat=1, fp32=False):
+        sec = ctypes.c_double()
+        st = lib().tflows_spmv_device(self._h, _ptr(val), _ptr(x), _ptr(y), int(repeat),
+                                      int(bool(fp32)), _stream(), ctypes.byref(sec))
+        if st != OK:
+            raise SolverError(st, last_error())
+        return sec.value
+
+    def pattern_outer(self, lam, x, grad):
+        st = lib().tflows_pattern_outer(self._h, _ptr(lam), _ptr(x), _ptr(grad), _stream())
+        if st != OK:
+            raise SolverError(st, last_error())
+        return grad

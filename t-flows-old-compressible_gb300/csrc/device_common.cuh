@@ -1,0 +1,258 @@
+// Device-side building blocks shared by the Krylov kernels (sm_103a).
+//
+// * memory-model helpers (relaxed / acquire / release accesses at gpu scope)
+// * a grid barrier for persistent cooperative launches whose every wait is
+//   bounded by %globaltimer and by a shared abort flag
+// * value-as-flag cells for the sync-free triangular sweeps: a cell holds a
+//   signalling-NaN sentinel until its producer stores the computed value
+//   (arithmetic never yields a signalling NaN, so a stored result can never
+//   be mistaken for the sentinel)
+// * deterministic block and grid reductions (fixed summation tree)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tflows {
+
+constexpr int kWarp = 32;
+
+// ---- status codes (mirror include/tflows_krylov.h) -------------------------
+enum : int {
+    ST_OK = 0, ST_NOT_CONVERGED = 1, ST_BREAKDOWN = 2, ST_NONFINITE = 3,
+    ST_TIMEOUT = 4, ST_BAD_INPUT = 5, ST_CUDA_ERROR = 6
+};
+
+// Exit kinds of the reference control flow (Process/CG.f90:69-72,105-108,255).
+enum : int { EXIT_BNRM = 1, EXIT_INIRES = 2, EXIT_CONVERGED = 3, EXIT_MAXITER = 4,
+             EXIT_ABORT = 5, EXIT_NONFINITE = 6 };
+
+// Per-solve device record (one per system), written by block 0.
+struct DevState {
+    int status;
+    int exit_kind;
+    int iterations;      // reference-visible iteration count
+    int inner_iters;     // mixed mode: total inner iterations
+    int refinements;     // mixed mode: refinement steps
+    int timeout_where;   // which wait timed out (diagnostics)
+    double ini_res;
+    double fin_res;
+    double bnrm2;
+    double pad[3];
+};
+
+// Control block shared by all blocks of one persistent launch.
+struct DevCtl {
+    unsigned long long bar;  // monotonically increasing arrival counter
+    int abort;               // set by whoever gives up; every wait checks it
+    int status;              // first error status raised
+    int where;
+    int pad;
+};
+
+__device__ __forceinline__ long long globaltimer_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ long long ld_relaxed_s64(const long long* p) {
+    long long v;
+    asm volatile("ld.relaxed.gpu.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_relaxed_s32(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_s64(long long* p, long long v) {
+    asm volatile("st.relaxed.gpu.global.s64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_s32(int* p, int v) {
+    asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Raise an abort: first status wins; everyone polling `abort` leaves.
+__device__ __forceinline__ void raise_abort(DevCtl* c, int status, int where) {
+    if (atomicCAS(&c->status, 0, status) == 0) c->where = where;
+    atomicExch(&c->abort, 1);
+}
+
+// ---- value-as-flag cells ------------------------------------------------------
+template <typename T> struct Cell;
+template <> struct Cell<double> {
+    using bits_t = long long;
+    static constexpr long long kSentinel = 0x7FF4242424242424LL;  // signalling NaN
+    __device__ static __forceinline__ bits_t bits(double v) { return __double_as_longlong(v); }
+    __device__ static __forceinline__ double value(bits_t b) { return __longlong_as_double(b); }
+    __device__ static __forceinline__ bits_t load(const double* p) {
+        return ld_relaxed_s64(reinterpret_cast<const long long*>(p));
+    }
+    __device__ static __forceinline__ void store(double* p, double v) {
+        st_relaxed_s64(reinterpret_cast<long long*>(p), __double_as_longlong(v));
+    }
+    __device__ static __forceinline__ double sentinel() { return __longlong_as_double(kSentinel); }
+};
+template <> struct Cell<float> {
+    using bits_t = int;
+    static constexpr int kSentinel = 0x7FA42424;  // signalling NaN
+    __device__ static __forceinline__ bits_t bits(float v) { return __float_as_int(v); }
+    __device__ static __forceinline__ float value(bits_t b) { return __int_as_float(b); }
+    __device__ static __forceinline__ bits_t load(const float* p) {
+        return ld_relaxed_s32(reinterpret_cast<const int*>(p));
+    }
+    __device__ static __forceinline__ void store(float* p, float v) {
+        st_relaxed_s32(reinterpret_cast<int*>(p), __float_as_int(v));
+    }
+    __device__ static __forceinline__ float sentinel() { return __int_as_float(kSentinel); }
+};
+
+// Wait until *p holds a produced value.  Bounded: gives up after
+// `timeout_ns` of waiting or when another thread raised the abort flag;
+// then returns false (the caller must stop its phase).
+template <typename T>
+__device__ __forceinline__ bool wait_cell(const T* p, T& out, DevCtl* ctl, long long timeout_ns,
+                                          int where) {
+    using C = Cell<T>;
+    auto b = C::load(p);
+    if (b != C::kSentinel) {
+        out = C::value(b);
+        return true;
+    }
+    long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    while (true) {
+        __nanosleep(40);
+        b = C::load(p);
+        if (b != C::kSentinel) {
+            out = C::value(b);
+            return true;
+        }
+        if ((++spins & 63u) == 0u) {
+            if (ld_relaxed_s32(&ctl->abort)) return false;
+            if (globaltimer_ns() - t0 > timeout_ns) {
+                raise_abort(ctl, ST_TIMEOUT, where);
+                return false;
+            }
+        }
+    }
+}
+
+// ---- reductions ---------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum K per-thread values over the block; thread 0 writes them to out[k].
+// `sm` must hold K * (blockDim.x / 32) doubles.
+template <int K>
+__device__ __forceinline__ void block_sums(const double (&v)[K], double* sm, double* out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = warp_sum(v[k]);
+        if (lane == 0) sm[k * nw + warp] = s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double s = lane < nw ? sm[k * nw + lane] : 0.0;
+            s = warp_sum(s);
+            if (lane == 0) out[k] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// Persistent-launch context kept in registers / shared memory of each block.
+struct Grid {
+    DevCtl* ctl;
+    double* partials;   // [slots][nblocks]
+    long long timeout_ns;
+    unsigned long long target;  // thread 0 only
+    int nblocks;
+    int wg;   // global warp index
+    int nw;   // warps in the grid
+    int lane;
+};
+
+// Grid-wide barrier with release/acquire ordering (every write before the
+// barrier is visible to every read after it).  Returns false when the
+// launch was aborted (timeout or error raised anywhere).
+__device__ __forceinline__ bool grid_sync(Grid& g, int where) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        g.target += (unsigned long long)g.nblocks;
+        __threadfence();
+        red_release_add_u64(&g.ctl->bar, 1ull);
+        int ok = 1;
+        long long t0 = 0;
+        unsigned spins = 0;
+        while (ld_acquire_u64(&g.ctl->bar) < g.target) {
+            if ((++spins & 255u) == 0u) {
+                if (ld_relaxed_s32(&g.ctl->abort)) { ok = 0; break; }
+                long long t = globaltimer_ns();
+                if (t0 == 0) t0 = t;
+                else if (t - t0 > g.timeout_ns) {
+                    raise_abort(g.ctl, ST_TIMEOUT, where);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        if (ld_relaxed_s32(&g.ctl->abort)) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Publish this block's K partial sums into slot range [slot, slot+K).
+template <int K>
+__device__ __forceinline__ void publish(Grid& g, int slot, const double (&v)[K]) {
+    __shared__ double sm[K * 32];
+    __shared__ double out[K];
+    block_sums<K>(v, sm, out);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) g.partials[(size_t)(slot + k) * g.nblocks + blockIdx.x] = out[k];
+    }
+}
+
+// After a grid_sync: every block computes the same K totals in the same
+// order (deterministic), broadcast through shared memory.
+template <int K>
+__device__ __forceinline__ void totals(Grid& g, int slot, double (&res)[K]) {
+    __shared__ double s_tot[K];
+    if ((threadIdx.x >> 5) == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const long long* src =
+                reinterpret_cast<const long long*>(g.partials + (size_t)(slot + k) * g.nblocks);
+            double s = 0.0;
+            for (int b = g.lane; b < g.nblocks; b += 32) s += __longlong_as_double(ld_relaxed_s64(src + b));
+            s = warp_sum(s);
+            if (g.lane == 0) s_tot[k] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) res[k] = s_tot[k];
+    __syncthreads();
+}
+
+}  // namespace tflows

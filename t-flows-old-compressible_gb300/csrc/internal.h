@@ -1,0 +1,107 @@
+// Internal host-side interfaces of libtflows_krylov.so (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace tflows {
+
+// A compressed-row pattern resident on one device, in SELL-32 form plus the
+// wavefront orders the IC(0) sweeps need.
+struct DeviceTopology {
+    int device = 0;
+    int n = 0;
+    int nnz = 0;
+    int nslices = 0;
+    long long sell_len = 0;
+    int max_len = 0;
+    bool ic_ok = false;        // lower part = slots before the diagonal, ascending
+    bool levels_built = false;
+    int nlev_f = 0, nlev_b = 0;
+    int nchunk_f = 0, nchunk_b = 0;
+    // device arrays
+    int* rowptr = nullptr;     // 0-based, n + 1
+    int* col = nullptr;        // 0-based, nnz
+    long long* soff = nullptr; // nslices + 1
+    int* scol = nullptr;       // sell_len
+    int* meta = nullptr;       // n: length | diag slot << 16
+    int* perm_f = nullptr;
+    int* perm_b = nullptr;
+    int* tpos = nullptr;       // transpose map (lazy)
+    // host copies (0-based) for lazy derived data
+    std::vector<int> h_rowptr, h_col, h_diag;
+};
+
+// Device buffers reused across solves of one context.
+struct Workspace {
+    int device = -1;
+    size_t vec_cap = 0;        // elements per vector (padded n)
+    size_t sell_cap = 0;       // SELL elements
+    int part_cap = 0;          // blocks
+    double* sval64 = nullptr;
+    float* sval32 = nullptr;
+    double* vec64 = nullptr;   // kVecs vectors of vec_cap doubles
+    float* vec32 = nullptr;    // kVecs vectors of vec_cap floats
+    double* csr_val = nullptr; // staging for host values (nnz)
+    size_t csr_cap = 0;
+    double* partials = nullptr;
+    void* ctl = nullptr;       // DevCtl
+    void* state = nullptr;     // DevState
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+constexpr int kVecs = 14;
+
+struct SolveRequest {
+    int method = 0;     // 0 CG, 1 BiCG, 2 CGS, 3 true BiCG
+    int prec = 0;
+    int precision = 0;  // 0 FP64, 1 mixed
+    int maxiter = 0;
+    double tol = 0.0;
+    int tol_relative = 0;
+    int x_is_zero = 0;
+    double inner_rtol = 1e-4;
+    int inner_maxiter = 1000;
+    int max_refinements = 30;
+    int ic_sweeps = 0;
+    double timeout_s = 5.0;
+    int block = 0;
+    int grid = 0;
+};
+
+struct SolveReport {
+    int status = 0;
+    int exit_kind = 0;
+    int iterations = 0;
+    int inner_iterations = 0;
+    int refinements = 0;
+    double ini_res = 0.0;
+    double fin_res = 0.0;
+    double seconds = 0.0;
+    double bytes = 0.0;
+    std::string message;
+};
+
+// krylov.cu
+cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t);
+void free_workspace(Workspace& ws);
+// Values (nnz FP64, stored order, device) -> SELL values (FP64 and/or FP32).
+cudaError_t permute_values(const DeviceTopology& t, Workspace& ws, const double* csr_val,
+                           bool want64, bool want32, cudaStream_t s);
+// Runs a full solve. x (n) and r (n, holds b on entry) are device FP64 arrays.
+int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
+              cudaStream_t s, SolveReport& rep);
+// Prec1 only: D (n, device FP64).
+int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, double timeout_s,
+              cudaStream_t s, SolveReport& rep);
+// r <- r - A x (Resid), device arrays.
+cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, double* r,
+                      cudaStream_t s);
+cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, double* y, bool fp32,
+                     int repeat, cudaStream_t s, float* ms);
+cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, const double* x,
+                              double* g, cudaStream_t s);
+
+}  // namespace tflows

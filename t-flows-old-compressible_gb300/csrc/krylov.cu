@@ -1,0 +1,407 @@
+// Kernels and launchers of libtflows_krylov.so.
+#include "internal.h"
+#include "krylov_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace tflows {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+template <typename T>
+struct KParams {
+    Mat<T> m;
+    Vecs<T> v;
+    SolveCfg cfg;
+    DevCtl* ctl;
+    DevState* state;
+    double* partials;
+    long long timeout_ns;
+    int mode;  // 0 solve, 1 Prec1 only
+};
+
+__device__ int status_of(const SolveOut& o, const DevCtl* ctl) {
+    if (ctl->status != 0) return ctl->status;
+    switch (o.exit_kind) {
+        case EXIT_MAXITER: return isfinite(o.fin_res) ? ST_NOT_CONVERGED : ST_NONFINITE;
+        case EXIT_NONFINITE: return ST_NONFINITE;
+        case EXIT_ABORT: return ST_TIMEOUT;
+        default: return ST_OK;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) krylov_kernel(KParams<T> P) {
+    Grid g;
+    g.ctl = P.ctl;
+    g.partials = P.partials;
+    g.timeout_ns = P.timeout_ns;
+    g.target = 0;
+    g.nblocks = gridDim.x;
+    g.lane = threadIdx.x & 31;
+    g.wg = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    g.nw = (int)((gridDim.x * blockDim.x) >> 5);
+    SolveOut out;
+    out.exit_kind = 0;
+    out.iterations = 0;
+    out.ini_res = 0.0;
+    out.fin_res = 0.0;
+    out.bnrm2 = 0.0;
+    if (P.mode == 1) {
+        bool ok = prec1_phase(g, P.m, P.v.D, P.cfg.prec);
+        out.exit_kind = ok ? EXIT_CONVERGED : EXIT_ABORT;
+    } else if (P.cfg.method == 2) {
+        cgs_solve(g, P.m, P.v, P.cfg, out);
+    } else {
+        cg_solve(g, P.m, P.v, P.cfg, out);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        DevState* s = P.state;
+        s->status = status_of(out, P.ctl);
+        s->exit_kind = out.exit_kind;
+        s->iterations = out.iterations;
+        s->ini_res = out.ini_res;
+        s->fin_res = out.fin_res;
+        s->bnrm2 = out.bnrm2;
+        s->timeout_where = P.ctl->where;
+    }
+}
+
+template <typename T>
+__global__ void fill_kernel(T* p, long long n, T v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+template <typename T>
+__global__ void fill_sentinel_kernel(T* p, long long n) {
+    const T v = Cell<T>::sentinel();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// SELL values from stored-order values: one thread per row.
+__global__ void permute_kernel(int n, const int* __restrict__ rowptr,
+                               const long long* __restrict__ soff, const double* __restrict__ val,
+                               double* __restrict__ s64, float* __restrict__ s32) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int b = rowptr[i], e = rowptr[i + 1];
+        const long long base = soff[i >> 5] + (i & 31);
+        for (int j = b; j < e; ++j) {
+            const double a = val[j];
+            const long long o = base + 32LL * (j - b);
+            if (s64) s64[o] = a;
+            if (s32) s32[o] = (float)a;
+        }
+    }
+}
+
+// Standalone SELL product (bandwidth measurement and tests).
+template <typename T, typename V>
+__global__ void __launch_bounds__(kBlock) spmv_kernel(Mat<T> m, const V* __restrict__ x,
+                                                      V* __restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int s = wg; s < m.nslices; s += nw) {
+        const T v = sell_row(m, s, lane, x);
+        const int i = s * kWarp + lane;
+        if (i < m.n) y[i] = V(v);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) resid_kernel(Mat<double> m, const double* __restrict__ x,
+                                                       double* __restrict__ r) {
+    const int lane = threadIdx.x & 31;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int s = wg; s < m.nslices; s += nw) {
+        const int i = s * kWarp + lane;
+        double ri = i < m.n ? r[i] : 0.0;
+        ri = sell_resid_row(m, s, lane, ri, x);
+        if (i < m.n) r[i] = ri;
+    }
+}
+
+__global__ void pattern_outer_kernel(int n, const int* __restrict__ rowptr,
+                                     const int* __restrict__ col, const double* __restrict__ lam,
+                                     const double* __restrict__ x, double* __restrict__ g) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double li = lam[i];
+        for (int j = rowptr[i]; j < rowptr[i + 1]; ++j) g[j] = -li * x[col[j]];
+    }
+}
+
+int g_num_sms = 0;
+int sms() {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    return g_num_sms;
+}
+
+template <typename T>
+Mat<T> make_mat(const DeviceTopology& t, const T* sval) {
+    Mat<T> m;
+    m.n = t.n;
+    m.nslices = t.nslices;
+    m.soff = t.soff;
+    m.scol = t.scol;
+    m.sval = sval;
+    m.meta = t.meta;
+    m.perm_f = t.perm_f;
+    m.perm_b = t.perm_b;
+    m.nchunk_f = t.nchunk_f;
+    m.nchunk_b = t.nchunk_b;
+    return m;
+}
+
+int blocks_for(int nslices) { return std::max(1, (nslices + kBlock / 32 - 1) / (kBlock / 32)); }
+
+}  // namespace
+
+cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t) {
+    cudaError_t e = cudaSuccess;
+    const size_t vec = (size_t)t.nslices * kWarp + 32;
+    if (vec > ws.vec_cap) {
+        if (ws.vec64) cudaFree(ws.vec64);
+        if (ws.vec32) cudaFree(ws.vec32);
+        ws.vec64 = nullptr;
+        ws.vec32 = nullptr;
+        if ((e = cudaMalloc(&ws.vec64, vec * kVecs * sizeof(double))) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&ws.vec32, vec * kVecs * sizeof(float))) != cudaSuccess) return e;
+        ws.vec_cap = vec;
+    }
+    const size_t sl = (size_t)t.sell_len;
+    if (sl > ws.sell_cap) {
+        if (ws.sval64) cudaFree(ws.sval64);
+        if (ws.sval32) cudaFree(ws.sval32);
+        ws.sval64 = nullptr;
+        ws.sval32 = nullptr;
+        if ((e = cudaMalloc(&ws.sval64, sl * sizeof(double))) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&ws.sval32, sl * sizeof(float))) != cudaSuccess) return e;
+        ws.sell_cap = sl;
+    }
+    if ((size_t)t.nnz > ws.csr_cap) {
+        if (ws.csr_val) cudaFree(ws.csr_val);
+        ws.csr_val = nullptr;
+        if ((e = cudaMalloc(&ws.csr_val, std::max<size_t>(t.nnz, 1) * sizeof(double))) != cudaSuccess)
+            return e;
+        ws.csr_cap = t.nnz;
+    }
+    if (!ws.partials) {
+        ws.part_cap = 64 * 1024;
+        if ((e = cudaMalloc(&ws.partials, (size_t)NUM_SLOTS * ws.part_cap * sizeof(double))) !=
+            cudaSuccess)
+            return e;
+        if ((e = cudaMalloc(&ws.ctl, sizeof(DevCtl))) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&ws.state, sizeof(DevState))) != cudaSuccess) return e;
+        cudaEventCreate(&ws.ev0);
+        cudaEventCreate(&ws.ev1);
+    }
+    // SELL padding slots are never read as values, but keep them defined.
+    return cudaSuccess;
+}
+
+void free_workspace(Workspace& ws) {
+    for (void* p : {(void*)ws.sval64, (void*)ws.sval32, (void*)ws.vec64, (void*)ws.vec32,
+                    (void*)ws.csr_val, (void*)ws.partials, ws.ctl, ws.state})
+        if (p) cudaFree(p);
+    if (ws.ev0) cudaEventDestroy(ws.ev0);
+    if (ws.ev1) cudaEventDestroy(ws.ev1);
+    ws = Workspace();
+}
+
+cudaError_t permute_values(const DeviceTopology& t, Workspace& ws, const double* csr_val,
+                           bool want64, bool want32, cudaStream_t s) {
+    const int nb = std::min(std::max(1, (t.n + 255) / 256), sms() * 16);
+    permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.soff, csr_val, want64 ? ws.sval64 : nullptr,
+                                      want32 ? ws.sval32 : nullptr);
+    return cudaGetLastError();
+}
+
+namespace {
+
+template <typename T>
+Vecs<T> carve(T* base, size_t cap, T* x, T* r) {
+    Vecs<T> v;
+    v.x = x;
+    v.r = r;
+    v.p = base + 0 * cap;
+    v.q = base + 1 * cap;
+    v.z = base + 2 * cap;
+    v.w = base + 3 * cap;
+    v.D = base + 4 * cap;
+    v.r2 = base + 5 * cap;
+    v.u1 = base + 6 * cap;
+    v.u2 = base + 7 * cap;
+    v.v2 = base + 8 * cap;
+    v.p2 = base + 9 * cap;
+    v.t = base + 10 * cap;
+    return v;
+}
+
+template <typename T>
+int max_coresident(int block) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, krylov_kernel<T>, block, 0);
+    return std::max(1, per_sm) * sms();
+}
+
+template <typename T>
+cudaError_t launch_persistent(KParams<T>& P, int grid, cudaStream_t s) {
+    void* args[] = {&P};
+    return cudaLaunchCooperativeKernel((const void*)krylov_kernel<T>, dim3(grid), dim3(kBlock), args,
+                                       0, s);
+}
+
+int choose_grid(const DeviceTopology& t, int requested, int max_blocks) {
+    int g = requested > 0 ? requested : blocks_for(t.nslices);
+    return std::max(1, std::min(g, std::min(max_blocks, 64 * 1024)));
+}
+
+}  // namespace
+
+int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, double timeout_s,
+              cudaStream_t s, SolveReport& rep) {
+    KParams<double> P;
+    std::memset(&P, 0, sizeof(P));
+    P.m = make_mat<double>(t, ws.sval64);
+    P.v = carve<double>(ws.vec64, ws.vec_cap, nullptr, nullptr);
+    P.v.D = D;
+    P.cfg.prec = prec;
+    P.ctl = (DevCtl*)ws.ctl;
+    P.state = (DevState*)ws.state;
+    P.partials = ws.partials;
+    P.timeout_ns = (long long)(timeout_s * 1e9);
+    P.mode = 1;
+    cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
+    const int grid = choose_grid(t, 0, max_coresident<double>(kBlock));
+    cudaError_t e = launch_persistent(P, grid, s);
+    if (e != cudaSuccess) {
+        rep.status = ST_CUDA_ERROR;
+        rep.message = cudaGetErrorString(e);
+        return rep.status;
+    }
+    DevState st;
+    e = cudaMemcpyAsync(&st, ws.state, sizeof(st), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        rep.status = ST_CUDA_ERROR;
+        rep.message = cudaGetErrorString(e);
+        return rep.status;
+    }
+    rep.status = st.status;
+    return rep.status;
+}
+
+int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
+              cudaStream_t s, SolveReport& rep) {
+    KParams<double> P;
+    std::memset(&P, 0, sizeof(P));
+    P.m = make_mat<double>(t, ws.sval64);
+    P.v = carve<double>(ws.vec64, ws.vec_cap, x, r);
+    P.cfg.method = rq.method == 2 ? 2 : 0;
+    P.cfg.prec = rq.prec;
+    P.cfg.maxiter = rq.maxiter;
+    P.cfg.tol = rq.tol;
+    P.cfg.x_is_zero = rq.x_is_zero;
+    P.cfg.do_prec1 = 1;
+    P.cfg.tol_is_relative = rq.tol_relative;
+    P.ctl = (DevCtl*)ws.ctl;
+    P.state = (DevState*)ws.state;
+    P.partials = ws.partials;
+    P.timeout_ns = (long long)(rq.timeout_s * 1e9);
+    P.mode = 0;
+    cudaError_t e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
+    if (rq.prec == 2) {
+        const long long nvec = (long long)t.nslices * kWarp;
+        fill_sentinel_kernel<double><<<std::min(1024, (int)((nvec + 255) / 256)), 256, 0, s>>>(P.v.w, nvec);
+    }
+    const int maxb = max_coresident<double>(kBlock);
+    const int grid = choose_grid(t, rq.grid, maxb);
+    cudaEventRecord(ws.ev0, s);
+    if (e == cudaSuccess) e = launch_persistent(P, grid, s);
+    cudaEventRecord(ws.ev1, s);
+    if (e != cudaSuccess) {
+        rep.status = ST_CUDA_ERROR;
+        rep.message = std::string("solver launch: ") + cudaGetErrorString(e);
+        return rep.status;
+    }
+    DevState st;
+    e = cudaMemcpyAsync(&st, ws.state, sizeof(st), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        rep.status = ST_CUDA_ERROR;
+        rep.message = std::string("solver: ") + cudaGetErrorString(e);
+        return rep.status;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ws.ev0, ws.ev1);
+    rep.status = st.status;
+    rep.exit_kind = st.exit_kind;
+    rep.iterations = st.iterations;
+    rep.ini_res = st.ini_res;
+    rep.fin_res = st.fin_res;
+    rep.seconds = ms * 1e-3;
+    // Algorithmic bytes: per iteration one SELL product (values + indices,
+    // each row's x gathered once) plus the vector passes of the schedule.
+    const double spmv = (double)t.nnz * (8.0 + 4.0) + 8.0 * (t.nslices + 1) + 16.0 * t.n;
+    const int it = std::max(0, std::min(st.iterations, rq.maxiter));
+    double per_it;
+    if (P.cfg.method == 2) per_it = 2 * spmv + 8.0 * t.n * 22;
+    else per_it = spmv + 8.0 * t.n * (rq.prec == 1 ? 12 : 10);
+    rep.bytes = per_it * it + spmv + 8.0 * t.n * 4;
+    if (st.status == ST_TIMEOUT)
+        rep.message = "device wait exceeded the timeout (site " + std::to_string(st.timeout_where) + ")";
+    return rep.status;
+}
+
+cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, double* r,
+                      cudaStream_t s) {
+    Mat<double> m = make_mat<double>(t, ws.sval64);
+    const int nb = std::min(blocks_for(t.nslices), sms() * 8);
+    resid_kernel<<<nb, kBlock, 0, s>>>(m, x, r);
+    return cudaGetLastError();
+}
+
+cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, double* y, bool fp32,
+                     int repeat, cudaStream_t s, float* ms) {
+    const int nb = std::min(blocks_for(t.nslices), sms() * 8);
+    cudaEventRecord(ws.ev0, s);
+    for (int k = 0; k < std::max(1, repeat); ++k) {
+        if (fp32) {
+            float* x32 = ws.vec32;
+            float* y32 = ws.vec32 + ws.vec_cap;
+            if (k == 0) {
+                // conversion outside the timed product is done by the caller
+            }
+            spmv_kernel<float, float><<<nb, kBlock, 0, s>>>(make_mat<float>(t, ws.sval32), x32, y32);
+        } else {
+            spmv_kernel<double, double><<<nb, kBlock, 0, s>>>(make_mat<double>(t, ws.sval64), x, y);
+        }
+    }
+    cudaEventRecord(ws.ev1, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaEventSynchronize(ws.ev1);
+    if (ms) cudaEventElapsedTime(ms, ws.ev0, ws.ev1);
+    return e;
+}
+
+cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, const double* x,
+                              double* g, cudaStream_t s) {
+    const int nb = std::min(std::max(1, (t.n + 255) / 256), sms() * 16);
+    pattern_outer_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.col, lambda, x, g);
+    return cudaGetLastError();
+}
+
+}  // namespace tflows

@@ -32,7 +32,7 @@ import numpy as np
 __all__ = [
     "System", "box_csr", "box_geometry", "pressure_system",
     "convection_diffusion_system", "config_system", "batch_sizes",
-    "side_c", "structured_levels",
+    "side_c", "interior_faces", "structured_levels",
 ]
 
 
@@ -58,10 +58,6 @@ class System:
     Ab: np.ndarray
     b: np.ndarray
     x: np.ndarray
-    c1: np.ndarray
-    c2: np.ndarray
-    pos12: np.ndarray
-    pos21: np.ndarray
     symmetric: bool
     rel_tol: float = 1e-8
     face_coef: np.ndarray | None = None
@@ -136,120 +132,212 @@ def box_csr(nx: int, ny: int, nz: int):
     return Acol, Arow, Adia, slot
 
 
-def _cross(a, b):
-    return np.stack([
-        a[..., 1] * b[..., 2] - a[..., 2] * b[..., 1],
-        a[..., 2] * b[..., 0] - a[..., 0] * b[..., 2],
-        a[..., 0] * b[..., 1] - a[..., 1] * b[..., 0],
-    ], axis=-1)
+class V3:
+    """Three same-shaped component arrays (structure of arrays): slicing,
+    +, -, scalar *, dot and cross act componentwise without ever stacking
+    the components into one (..., 3) array."""
+
+    __slots__ = ("x", "y", "z")
+
+    def __init__(self, x, y, z):
+        self.x, self.y, self.z = x, y, z
+
+    def __getitem__(self, idx):
+        return V3(self.x[idx], self.y[idx], self.z[idx])
+
+    def __add__(self, o):
+        return V3(self.x + o.x, self.y + o.y, self.z + o.z)
+
+    def __sub__(self, o):
+        return V3(self.x - o.x, self.y - o.y, self.z - o.z)
+
+    def __mul__(self, k):
+        return V3(self.x * k, self.y * k, self.z * k)
+
+    __rmul__ = __mul__
+
+    def dot(self, o):
+        return self.x * o.x + self.y * o.y + self.z * o.z
+
+    def cross(self, o):
+        return V3(self.y * o.z - self.z * o.y, self.z * o.x - self.x * o.z,
+                  self.x * o.y - self.y * o.x)
+
+    def ravel(self):
+        return V3(self.x.ravel(), self.y.ravel(), self.z.ravel())
 
 
 def _dot(a, b):
-    return np.einsum("...i,...i->...", a, b)
+    return a.dot(b)
 
 
 def box_geometry(nx, ny, nz, h=1.0, perturb=0.0, rng=None):
     """Node, face and cell geometry of a (perturbed) hex box.
 
-    Nodes are displaced by ``uniform(-perturb*h, perturb*h)`` per coordinate.
-    Face area vectors are ``0.5 * (c - a) x (d - b)`` for the quad a-b-c-d,
-    oriented along +x, +y, +z; cell volumes come from the divergence theorem.
-    Returns a dict with node array ``P`` (nz+1, ny+1, nx+1, 3), face arrays
-    ``Sx, Sy, Sz`` and face centres ``Fx, Fy, Fz``, cell centres ``C`` and
-    volumes ``V`` (nz, ny, nx).
+    Nodes are displaced by ``uniform(-perturb*h, perturb*h)`` per coordinate
+    (one draw of shape (nz+1, ny+1, nx+1, 3)).  Face area vectors are
+    ``0.5 * (c - a) x (d - b)`` for the quad a-b-c-d, oriented along +x, +y,
+    +z; cell volumes come from the divergence theorem.  Returns a dict of
+    V3 arrays: nodes ``P`` (nz+1, ny+1, nx+1), face vectors ``Sx, Sy, Sz``
+    and face centres ``Fx, Fy, Fz``, cell centres ``C``, and volumes ``V``
+    (nz, ny, nx).
     """
-    z, y, x = np.meshgrid(np.arange(nz + 1), np.arange(ny + 1), np.arange(nx + 1),
-                          indexing="ij")
-    P = np.stack([x, y, z], axis=-1).astype(np.float64) * h
-    del x, y, z
+    shape = (nz + 1, ny + 1, nx + 1)
+    X = np.broadcast_to(np.arange(nx + 1, dtype=np.float64)[None, None, :] * h, shape).copy()
+    Y = np.broadcast_to(np.arange(ny + 1, dtype=np.float64)[None, :, None] * h, shape).copy()
+    Z = np.broadcast_to(np.arange(nz + 1, dtype=np.float64)[:, None, None] * h, shape).copy()
     if perturb > 0.0:
-        P += rng.uniform(-perturb * h, perturb * h, size=P.shape)
+        d = rng.uniform(-perturb * h, perturb * h, size=shape + (3,))
+        X += d[..., 0]
+        Y += d[..., 1]
+        Z += d[..., 2]
+        del d
+    P = V3(X, Y, Z)
+
+    def quad(a, b_, c, d):
+        return 0.5 * (c - a).cross(d - b_), 0.25 * (a + b_ + c + d)
+
     # x-faces on node plane i: a=(k,j), b=(k,j+1), c=(k+1,j+1), d=(k+1,j)
-    a, b_, c, d = P[:-1, :-1, :], P[:-1, 1:, :], P[1:, 1:, :], P[1:, :-1, :]
-    Sx = 0.5 * _cross(c - a, d - b_)
-    Fx = 0.25 * (a + b_ + c + d)
+    Sx, Fx = quad(P[:-1, :-1, :], P[:-1, 1:, :], P[1:, 1:, :], P[1:, :-1, :])
     # y-faces on node plane j: a=(k,i), b=(k+1,i), c=(k+1,i+1), d=(k,i+1)
-    a, b_, c, d = P[:-1, :, :-1], P[1:, :, :-1], P[1:, :, 1:], P[:-1, :, 1:]
-    Sy = 0.5 * _cross(c - a, d - b_)
-    Fy = 0.25 * (a + b_ + c + d)
+    Sy, Fy = quad(P[:-1, :, :-1], P[1:, :, :-1], P[1:, :, 1:], P[:-1, :, 1:])
     # z-faces on node plane k: a=(j,i), b=(j,i+1), c=(j+1,i+1), d=(j+1,i)
-    a, b_, c, d = P[:, :-1, :-1], P[:, :-1, 1:], P[:, 1:, 1:], P[:, 1:, :-1]
-    Sz = 0.5 * _cross(c - a, d - b_)
-    Fz = 0.25 * (a + b_ + c + d)
-    del a, b_, c, d
+    Sz, Fz = quad(P[:, :-1, :-1], P[:, :-1, 1:], P[:, 1:, 1:], P[:, 1:, :-1])
     C = 0.125 * (P[:-1, :-1, :-1] + P[:-1, :-1, 1:] + P[:-1, 1:, :-1] + P[:-1, 1:, 1:]
                  + P[1:, :-1, :-1] + P[1:, :-1, 1:] + P[1:, 1:, :-1] + P[1:, 1:, 1:])
-    fx, fy, fz = _dot(Fx, Sx), _dot(Fy, Sy), _dot(Fz, Sz)
-    V = (fx[:, :, 1:] - fx[:, :, :-1] + fy[:, 1:, :] - fy[:, :-1, :]
-         + fz[1:, :, :] - fz[:-1, :, :]) / 3.0
-    return dict(P=P, Sx=Sx, Sy=Sy, Sz=Sz, Fx=Fx, Fy=Fy, Fz=Fz, C=C, V=V)
+    fx, fy, fz = Fx.dot(Sx), Fy.dot(Sy), Fz.dot(Sz)
+    Vol = (fx[:, :, 1:] - fx[:, :, :-1] + fy[:, 1:, :] - fy[:, :-1, :]
+           + fz[1:, :, :] - fz[:-1, :, :]) / 3.0
+    return dict(P=P, Sx=Sx, Sy=Sy, Sz=Sz, Fx=Fx, Fy=Fy, Fz=Fz, C=C, V=Vol)
 
 
-def _interior_faces(nx, ny, nz, slot, geo):
-    """Interior faces in SideC order with SidAij positions and geometry."""
-    N = nx * ny * nz
-    cell = np.arange(N, dtype=np.int64).reshape(nz, ny, nx)
+# Slot order of a 7-point row (ascending column offset): -z, -y, -x, diag,
+# +x, +y, +z; the (c1, c2) entry of an axis-d face sits in slot PLUS[d] of
+# row c1 and the (c2, c1) entry in slot MINUS[d] of row c2.
+PLUS = (4, 5, 6)
+MINUS = (2, 1, 0)
+DIAG = 3
+
+
+def _face_slices(axis):
+    """(lo, hi) index tuples over the (nz, ny, nx) cell grid selecting the
+    lower / upper cell of every interior face normal to `axis`."""
+    lo = [slice(None)] * 3
+    hi = [slice(None)] * 3
+    dim = 2 - axis
+    lo[dim] = slice(0, -1)
+    hi[dim] = slice(1, None)
+    return tuple(lo), tuple(hi)
+
+
+def _interior_geometry(geo, axis):
+    """Area vectors and centre-to-centre vectors of the interior faces normal
+    to `axis`, shaped like the face grid."""
+    S = (geo["Sx"][:, :, 1:-1], geo["Sy"][:, 1:-1, :], geo["Sz"][1:-1])[axis]
+    lo, hi = _face_slices(axis)
     C = geo["C"]
-    out = []
-    for axis, off, sl_lo, sl_hi, S in (
-        (0, 1, (slice(None), slice(None), slice(0, nx - 1)),
-         (slice(None), slice(None), slice(1, nx)), geo["Sx"][:, :, 1:nx]),
-        (1, nx, (slice(None), slice(0, ny - 1), slice(None)),
-         (slice(None), slice(1, ny), slice(None)), geo["Sy"][:, 1:ny, :]),
-        (2, nx * ny, (slice(0, nz - 1), slice(None), slice(None)),
-         (slice(1, nz), slice(None), slice(None)), geo["Sz"][1:nz, :, :]),
-    ):
-        c1 = cell[sl_lo].ravel()
-        c2 = c1 + off
-        d = (C[sl_hi] - C[sl_lo]).reshape(-1, 3)
-        S = S.reshape(-1, 3)
-        out.append((c1, c2, slot[(axis, 1)][c1], slot[(axis, -1)][c2], S, d))
-    cat = lambda n: np.concatenate([o[n] for o in out])  # noqa: E731
-    return cat(0), cat(1), cat(2).astype(np.int64) - 1, cat(3).astype(np.int64) - 1, cat(4), cat(5)
+    return S, C[hi] - C[lo]
+
+
+class _SlotMatrix:
+    """Dense (nz, ny, nx, 7) slot array compressed into the TopolM layout."""
+
+    def __init__(self, nx, ny, nz):
+        self.shape = (nx, ny, nz)
+        self.A7 = np.zeros((nz, ny, nx, 7))
+
+    def face(self, axis, off12, off21, d1, d2):
+        """Add one direction's interior faces: entry (c1,c2) = -off12,
+        entry (c2,c1) = -off21, diag(c1) += d1, diag(c2) += d2."""
+        lo, hi = _face_slices(axis)
+        self.A7[lo + (PLUS[axis],)] -= off12
+        self.A7[hi + (MINUS[axis],)] -= off21
+        self.A7[lo + (DIAG,)] += d1
+        self.A7[hi + (DIAG,)] += d2
+
+    def diag(self):
+        return self.A7[..., DIAG]
+
+    def compress(self):
+        nx, ny, nz = self.shape
+        Acol, Arow, Adia, _ = box_csr(nx, ny, nz)
+        k = np.arange(nz)[:, None, None]
+        j = np.arange(ny)[None, :, None]
+        i = np.arange(nx)[None, None, :]
+        mask = np.empty((nz, ny, nx, 7), bool)
+        mask[..., 0] = k > 0
+        mask[..., 1] = j > 0
+        mask[..., 2] = i > 0
+        mask[..., 3] = True
+        mask[..., 4] = i < nx - 1
+        mask[..., 5] = j < ny - 1
+        mask[..., 6] = k < nz - 1
+        A = np.zeros(Arow.shape[0])
+        A[:-1] = self.A7[mask]
+        return A, Acol, Arow, Adia
 
 
 def _wall_faces(nx, ny, nz, geo):
     """Boundary faces (x-min, x-max, y-min, y-max, z-min, z-max) with the
-    adjacent cell, outward area vector and centre-to-face vector."""
+    adjacent cell, outward area vector and centre-to-face vector (V3)."""
     N = nx * ny * nz
     cell = np.arange(N, dtype=np.int64).reshape(nz, ny, nx)
     C = geo["C"]
-    res = []
-    for S, F, cidx, sign in (
-        (geo["Sx"][:, :, 0], geo["Fx"][:, :, 0], cell[:, :, 0], -1.0),
-        (geo["Sx"][:, :, nx], geo["Fx"][:, :, nx], cell[:, :, nx - 1], 1.0),
-        (geo["Sy"][:, 0, :], geo["Fy"][:, 0, :], cell[:, 0, :], -1.0),
-        (geo["Sy"][:, ny, :], geo["Fy"][:, ny, :], cell[:, ny - 1, :], 1.0),
-        (geo["Sz"][0], geo["Fz"][0], cell[0], -1.0),
-        (geo["Sz"][nz], geo["Fz"][nz], cell[nz - 1], 1.0),
+    cs, Ss, ds = [], [], []
+    for S, F, cidx, cc, sign in (
+        (geo["Sx"][:, :, 0], geo["Fx"][:, :, 0], cell[:, :, 0], C[:, :, 0], -1.0),
+        (geo["Sx"][:, :, nx], geo["Fx"][:, :, nx], cell[:, :, nx - 1], C[:, :, nx - 1], 1.0),
+        (geo["Sy"][:, 0, :], geo["Fy"][:, 0, :], cell[:, 0, :], C[:, 0, :], -1.0),
+        (geo["Sy"][:, ny, :], geo["Fy"][:, ny, :], cell[:, ny - 1, :], C[:, ny - 1, :], 1.0),
+        (geo["Sz"][0], geo["Fz"][0], cell[0], C[0], -1.0),
+        (geo["Sz"][nz], geo["Fz"][nz], cell[nz - 1], C[nz - 1], 1.0),
     ):
-        c = cidx.ravel()
-        Sout = sign * S.reshape(-1, 3)
-        d = F.reshape(-1, 3) - C.reshape(-1, 3)[c]
-        res.append((c, Sout, d))
-    return (np.concatenate([r[0] for r in res]), np.concatenate([r[1] for r in res]),
-            np.concatenate([r[2] for r in res]))
+        cs.append(cidx.ravel())
+        Ss.append((S * sign).ravel())
+        ds.append((F - cc).ravel())
+    cat = lambda vs: V3(*(np.concatenate([getattr(v, a) for v in vs]) for a in "xyz"))  # noqa
+    return np.concatenate(cs), cat(Ss), cat(ds)
+
+
+def interior_faces(nx, ny, nz):
+    """Interior faces in SideC order (x-, y-, z-faces, each in cell order):
+    0-based cells c1 < c2 and 0-based positions of entries (c1,c2) in row c1
+    and (c2,c1) in row c2 (the reference's SidAij minus 1)."""
+    N = nx * ny * nz
+    _, _, _, slot = box_csr(nx, ny, nz)
+    cell = np.arange(N, dtype=np.int64).reshape(nz, ny, nx)
+    c1s, c2s, p12s, p21s = [], [], [], []
+    for axis, off in ((0, 1), (1, nx), (2, nx * ny)):
+        lo, _ = _face_slices(axis)
+        c1 = cell[lo].ravel()
+        c2 = c1 + off
+        c1s.append(c1)
+        c2s.append(c2)
+        p12s.append(slot[(axis, 1)][c1].astype(np.int64) - 1)
+        p21s.append(slot[(axis, -1)][c2].astype(np.int64) - 1)
+    return (np.concatenate(c1s), np.concatenate(c2s), np.concatenate(p12s),
+            np.concatenate(p21s))
 
 
 def side_c(nx, ny, nz):
     """The face list as the reference stores it: SideC(2,NS), 1-based cells,
-    boundary faces with negative second cell (-1, -2, ...)."""
-    Acol, Arow, Adia, slot = box_csr(nx, ny, nz)
-    geo = dict(C=np.zeros((nz, ny, nx, 3)), Sx=np.zeros((nz, ny, nx + 1, 3)),
-               Sy=np.zeros((nz, ny + 1, nx, 3)), Sz=np.zeros((nz + 1, ny, nx, 3)),
-               Fx=np.zeros((nz, ny, nx + 1, 3)), Fy=np.zeros((nz, ny + 1, nx, 3)),
-               Fz=np.zeros((nz + 1, ny, nx, 3)))
-    c1, c2, p12, p21, _, _ = _interior_faces(nx, ny, nz, slot, geo)
-    cw, _, _ = _wall_faces(nx, ny, nz, geo)
+    boundary faces with negative second cell (-1, -2, ...), plus the layout
+    TopolM would build from it (Acol, Arow, Adia, SidAij(NS,2))."""
+    Acol, Arow, Adia, _ = box_csr(nx, ny, nz)
+    c1, c2, p12, p21 = interior_faces(nx, ny, nz)
+    cell = np.arange(nx * ny * nz, dtype=np.int64).reshape(nz, ny, nx)
+    cw = np.concatenate([cell[:, :, 0].ravel(), cell[:, :, nx - 1].ravel(), cell[:, 0, :].ravel(),
+                         cell[:, ny - 1, :].ravel(), cell[0].ravel(), cell[nz - 1].ravel()])
     nb = cw.shape[0]
-    sc = np.empty((c1.shape[0] + nb, 2), np.int32)
-    sc[: c1.shape[0], 0] = c1 + 1
-    sc[: c1.shape[0], 1] = c2 + 1
-    sc[c1.shape[0]:, 0] = cw + 1
-    sc[c1.shape[0]:, 1] = -np.arange(1, nb + 1)
+    ni = c1.shape[0]
+    sc = np.empty((ni + nb, 2), np.int32)
+    sc[:ni, 0] = c1 + 1
+    sc[:ni, 1] = c2 + 1
+    sc[ni:, 0] = cw + 1
+    sc[ni:, 1] = -np.arange(1, nb + 1)
     sid = np.zeros((sc.shape[0], 2), np.int32)
-    sid[: c1.shape[0], 0] = p12 + 1
-    sid[: c1.shape[0], 1] = p21 + 1
+    sid[:ni, 0] = p12 + 1
+    sid[:ni, 1] = p21 + 1
     return sc, (Acol, Arow, Adia, sid)
 
 
@@ -265,21 +353,12 @@ def _density(shape, rng, lo=0.14, hi=1.0, sigma=3.0):
     return lo + (hi - lo) * f
 
 
-def _assemble(N, NONZ, Adia, c1, c2, pos12, pos21, a12_off, a21_off, d1_add, d2_add,
-              diag_extra):
-    A = np.zeros(NONZ, np.float64)
-    A[pos12] = -a12_off
-    A[pos21] = -a21_off
-    diag = np.zeros(N, np.float64)
-    diag += np.bincount(c1, weights=d1_add, minlength=N)
-    diag += np.bincount(c2, weights=d2_add, minlength=N)
-    diag += diag_extra
-    A[Adia.astype(np.int64) - 1] = diag
-    return A
+def _geom_coef(S, d):
+    return _dot(S, S) / _dot(S, d)
 
 
 def pressure_system(nx, ny, nz, perturb=0.0, seed=0, variable_density=False,
-                    rel_tol=1e-8, name=None):
+                    rel_tol=1e-8, name=None, keep_faces=False):
     """Pressure-correction matrix (Process/CalcPS.f90:77-102 pattern).
 
     A12 = |S|^2/(S.d) (divided by the harmonic face density when
@@ -287,36 +366,45 @@ def pressure_system(nx, ny, nz, perturb=0.0, seed=0, variable_density=False,
     x-min wall coefficient added to the diagonal).  RHS ~ uniform[-1, 1]
     (``numpy.random.default_rng(seed)``), mean removed; x0 = 0.
     Random draws in order: node perturbation, density field, RHS.
+    With ``keep_faces`` the per-face coefficients are kept (interior_faces
+    order) together with the fixed diagonal part, for differentiable
+    assembly.
     """
     rng = np.random.default_rng(seed)
     N = nx * ny * nz
-    Acol, Arow, Adia, slot = box_csr(nx, ny, nz)
-    NONZ = int(Arow.shape[0])
     geo = box_geometry(nx, ny, nz, perturb=perturb, rng=rng)
-    c1, c2, p12, p21, S, d = _interior_faces(nx, ny, nz, slot, geo)
-    g = _dot(S, S) / _dot(S, d)
-    if variable_density:
-        rho = _density((nz, ny, nx), rng).ravel()
-        inv_rho_f = 0.5 * (1.0 / rho[c1] + 1.0 / rho[c2])
-    else:
-        rho = np.ones(N)
-        inv_rho_f = np.ones_like(g)
-    coef = g * inv_rho_f
-    cw, Sw, dw = _wall_faces(nx, ny, nz, geo)
-    NB = int(cw.shape[0])
-    diag_extra = np.zeros(N)
-    # Dirichlet face: the first wall face (x-min) of cell 1.
-    gw0 = float(_dot(Sw[0], Sw[0]) / _dot(Sw[0], dw[0]))
-    diag_extra[cw[0]] += gw0 / rho[cw[0]]
-    A = _assemble(N, NONZ, Adia, c1, c2, p12, p21, coef, coef, coef, coef, diag_extra)
+    rho = _density((nz, ny, nx), rng) if variable_density else None
+    M = _SlotMatrix(nx, ny, nz)
+    coefs = []
+    for axis in range(3):
+        S, d = _interior_geometry(geo, axis)
+        c = _geom_coef(S, d)
+        if rho is not None:
+            lo, hi = _face_slices(axis)
+            c = c * (0.5 * (1.0 / rho[lo] + 1.0 / rho[hi]))
+        M.face(axis, c, c, c, c)
+        if keep_faces:
+            coefs.append(c.ravel())
+    # Dirichlet face: the x-min wall of cell 1.
+    S0 = geo["Sx"][0, 0, 0]
+    d0 = geo["C"][0, 0, 0] - geo["Fx"][0, 0, 0]
+    gw0 = float(S0.dot(S0) / abs(S0.dot(d0)))
+    fixed = np.zeros(N)
+    fixed[0] = gw0 / (rho[0, 0, 0] if rho is not None else 1.0)
+    M.diag().reshape(-1)[0] += fixed[0]
+    NB = 2 * (nx * ny + ny * nz + nx * nz)
+    del geo
+    A, Acol, Arow, Adia = M.compress()
+    del M
     b = rng.uniform(-1.0, 1.0, N)
     b -= b.mean()
     x = np.zeros(NB + N + 1)
     return System(
         name=name or f"pressure{'-vd' if variable_density else ''}-{nx}x{ny}x{nz}",
-        shape=(nx, ny, nz), N=N, NB=NB, NONZ=NONZ, A=A, Acol=Acol, Arow=Arow,
-        Adia=Adia, Ab=np.zeros(NB), b=b, x=x, c1=c1, c2=c2, pos12=p12, pos21=p21,
-        symmetric=True, rel_tol=rel_tol, face_coef=coef, fixed_diag=diag_extra)
+        shape=(nx, ny, nz), N=N, NB=NB, NONZ=int(Arow.shape[0]), A=A, Acol=Acol, Arow=Arow,
+        Adia=Adia, Ab=np.zeros(NB), b=b, x=x, symmetric=True, rel_tol=rel_tol,
+        face_coef=np.concatenate(coefs) if keep_faces else None,
+        fixed_diag=fixed if keep_faces else None)
 
 
 def convection_diffusion_system(nx, ny, nz, perturb=0.2, seed=0, nu=1e-2, dt=1e-2,
@@ -337,58 +425,70 @@ def convection_diffusion_system(nx, ny, nz, perturb=0.2, seed=0, nu=1e-2, dt=1e-
     """
     rng = np.random.default_rng(seed)
     N = nx * ny * nz
-    Acol, Arow, Adia, slot = box_csr(nx, ny, nz)
-    NONZ = int(Arow.shape[0])
     geo = box_geometry(nx, ny, nz, perturb=perturb, rng=rng)
     P = geo["P"]
-    psi = np.stack([_smooth_field(P.shape[:3], sigma, rng) for _ in range(3)], axis=-1)
-    psi[0] = psi[-1] = 0.0
-    psi[:, 0] = psi[:, -1] = 0.0
-    psi[:, :, 0] = psi[:, :, -1] = 0.0
+    comps = []
+    for _ in range(3):
+        f = _smooth_field(P.x.shape, sigma, rng)
+        f[0] = f[-1] = 0.0
+        f[:, 0] = f[:, -1] = 0.0
+        f[:, :, 0] = f[:, :, -1] = 0.0
+        comps.append(f)
+    psi = V3(*comps)
+    del comps
 
     def circ(a, b_, c, d, pa, pb, pc, pd):
-        return (_dot(0.5 * (pa + pb), b_ - a) + _dot(0.5 * (pb + pc), c - b_)
-                + _dot(0.5 * (pc + pd), d - c) + _dot(0.5 * (pd + pa), a - d))
+        return ((pa + pb).dot(b_ - a) + (pb + pc).dot(c - b_) + (pc + pd).dot(d - c)
+                + (pd + pa).dot(a - d)) * 0.5
 
     # Same quad orderings as box_geometry, so the circulation is the flux
-    # through the oriented area vector (Stokes).
-    Gx = circ(P[:-1, :-1, :], P[:-1, 1:, :], P[1:, 1:, :], P[1:, :-1, :],
-              psi[:-1, :-1, :], psi[:-1, 1:, :], psi[1:, 1:, :], psi[1:, :-1, :])
-    Gy = circ(P[:-1, :, :-1], P[1:, :, :-1], P[1:, :, 1:], P[:-1, :, 1:],
-              psi[:-1, :, :-1], psi[1:, :, :-1], psi[1:, :, 1:], psi[:-1, :, 1:])
-    Gz = circ(P[:, :-1, :-1], P[:, :-1, 1:], P[:, 1:, 1:], P[:, 1:, :-1],
-              psi[:, :-1, :-1], psi[:, :-1, 1:], psi[:, 1:, 1:], psi[:, 1:, :-1])
+    # through the oriented area vector (Stokes).  Interior faces only.
+    F = [
+        circ(P[:-1, :-1, 1:-1], P[:-1, 1:, 1:-1], P[1:, 1:, 1:-1], P[1:, :-1, 1:-1],
+             psi[:-1, :-1, 1:-1], psi[:-1, 1:, 1:-1], psi[1:, 1:, 1:-1], psi[1:, :-1, 1:-1]),
+        circ(P[:-1, 1:-1, :-1], P[1:, 1:-1, :-1], P[1:, 1:-1, 1:], P[:-1, 1:-1, 1:],
+             psi[:-1, 1:-1, :-1], psi[1:, 1:-1, :-1], psi[1:, 1:-1, 1:], psi[:-1, 1:-1, 1:]),
+        circ(P[1:-1, :-1, :-1], P[1:-1, :-1, 1:], P[1:-1, 1:, 1:], P[1:-1, 1:, :-1],
+             psi[1:-1, :-1, :-1], psi[1:-1, :-1, 1:], psi[1:-1, 1:, 1:], psi[1:-1, 1:, :-1]),
+    ]
     del psi
-    F = np.concatenate([Gx[:, :, 1:nx].ravel(), Gy[:, 1:ny, :].ravel(), Gz[1:nz].ravel()])
-    c1, c2, p12, p21, S, d = _interior_faces(nx, ny, nz, slot, geo)
-    area = np.sqrt(_dot(S, S))
-    rms = math.sqrt(float(np.mean((F / area) ** 2))) if F.size else 1.0
-    F = F / max(rms, 1e-300)
-    if variable_density:
-        rho = _density((nz, ny, nx), rng).ravel()
-    else:
-        rho = np.ones(N)
-    A0 = nu * _dot(S, S) / _dot(S, d)
-    a12 = np.maximum(-F, 0.0)
-    a21 = np.maximum(F, 0.0)
-    D12 = A0 / rho[c2]
-    D21 = A0 / rho[c1]
+    geoms = [_interior_geometry(geo, a) for a in range(3)]
+    ssum, cnt = 0.0, 0
+    for a in range(3):
+        area2 = _dot(geoms[a][0], geoms[a][0])
+        ssum += float(np.sum(F[a] * F[a] / area2))
+        cnt += F[a].size
+    rms = math.sqrt(ssum / cnt) if cnt else 1.0
+    rho = _density((nz, ny, nx), rng) if variable_density else np.ones((nz, ny, nx))
+    M = _SlotMatrix(nx, ny, nz)
+    for a in range(3):
+        S, d = geoms[a]
+        Fa = F[a] / max(rms, 1e-300)
+        A0 = nu * _geom_coef(S, d)
+        lo, hi = _face_slices(a)
+        a12 = np.maximum(-Fa, 0.0)
+        a21 = np.maximum(Fa, 0.0)
+        D12 = A0 / rho[hi]
+        D21 = A0 / rho[lo]
+        M.face(a, a12 + D12, a21 + D21, a21 + D21, a12 + D12)
+    del F, geoms
     cw, Sw, dw = _wall_faces(nx, ny, nz, geo)
     NB = int(cw.shape[0])
+    rho_f = rho.ravel()
     V = geo["V"].ravel()
-    diag_extra = np.zeros(N, np.float64)
-    diag_extra += np.bincount(cw, weights=nu * _dot(Sw, Sw) / _dot(Sw, dw) / rho[cw],
-                              minlength=N)
-    diag_extra += rho * V / dt
-    A = _assemble(N, NONZ, Adia, c1, c2, p12, p21, a12 + D12, a21 + D21, a21 + D21,
-                  a12 + D12, diag_extra)
+    diag = M.diag().reshape(-1)
+    diag += np.bincount(cw, weights=nu * _dot(Sw, Sw) / _dot(Sw, dw) / rho_f[cw], minlength=N)
+    diag += rho_f * V / dt
+    del geo
+    A, Acol, Arow, Adia = M.compress()
+    del M
     u_old = rng.uniform(-1.0, 1.0, N)
-    b = rho * V / dt * u_old
+    b = rho_f * V / dt * u_old
     x = np.zeros(NB + N + 1)
     return System(
         name=name or f"convdiff-{nx}x{ny}x{nz}", shape=(nx, ny, nz), N=N, NB=NB,
-        NONZ=NONZ, A=A, Acol=Acol, Arow=Arow, Adia=Adia, Ab=np.zeros(NB), b=b, x=x,
-        c1=c1, c2=c2, pos12=p12, pos21=p21, symmetric=False, rel_tol=rel_tol)
+        NONZ=int(Arow.shape[0]), A=A, Acol=Acol, Arow=Arow, Adia=Adia, Ab=np.zeros(NB), b=b, x=x,
+        symmetric=False, rel_tol=rel_tol)
 
 
 def config_system(index: int, scale: int | None = None, seed: int = 0) -> System:
