@@ -175,6 +175,28 @@ int tflows_spmv_device(tflows_topology *topo, const double *val,
                        const double *x, double *y, int repeat, int fp32,
                        void *stream, double *sec);
 
+/* ---- allocation-free solve ------------------------------------------------ */
+/* No counterpart in the reference.  For callers that may not allocate GPU
+ * memory while they run (device memory reserved up front by another
+ * allocator, a fixed memory budget, or no room for the device-wide
+ * synchronisation of cudaMalloc/cudaFree): CG as in Process/CG.f90 with
+ * prec 1 (diagonal) or any other value but 2 (none) on device arrays -- a
+ * 0-based compressed-row matrix (rowptr n+1, col, diag, val), b, x (in/out)
+ * and r_out (final recursive residual, may be NULL) -- that allocates
+ * nothing.  Its work vectors live in one static device array of about
+ * 10.2 MB that every GPU loading the library keeps until exit; n is limited
+ * to 262144 rows (larger: TFLOWS_BAD_INPUT; prec 2: TFLOWS_UNSUPPORTED).
+ * All calls share that array, so calls that overlap on the GPU race.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress)
+ * and should come before any stream capture.  The pattern is not checked.
+ * Returns the status; *iterations, *ini_res, *fin_res as in tflows_cg (on the
+ * ||b|| < tol exit *ini_res and *fin_res are left as they were). */
+int tflows_cg_noalloc(int n, const int *rowptr, const int *col,
+                      const int *diag, const double *val, const double *b,
+                      double *x, double *r_out, int prec, int maxiter,
+                      double tol, void *stream, int *iterations,
+                      double *ini_res, double *fin_res);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libtflows_krylov.so")
-SOURCES = ("krylov.cu", "shim.cu")
+SOURCES = ("krylov.cu", "shim.cu", "noalloc.cu")
 HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "internal.h")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -132,6 +132,8 @@ SIGNATURES = {
     "tflows_pattern_outer": ([_VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "tflows_spmv_device": ([_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP,
                             ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "tflows_cg_noalloc": ([ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
+                           ctypes.c_int, ctypes.c_double, _VP, _I, _D, _D], ctypes.c_int),
 }
 
 
