@@ -172,11 +172,70 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def workload_config(s, method, prec):
-    return {"workload": "cfg2 convection-diffusion 128^3 perturbed hex, BiCG + diagonal, FP64, "
-                        "tol 1e-8*||b|| (absolute, reference test), x0=0",
-            "n": s.N, "nnz": s.nnz, "method": method, "prec": prec,
+def workload_config(s, method, prec, precision="fp64"):
+    return {"workload": f"{s.name}: BiCG/CG solve to 1e-8*||b|| (absolute test as the reference), "
+                        f"x0=0, {method}, prec {prec}, {precision}",
+            "n": s.N, "nnz": s.nnz, "method": method, "prec": prec, "precision": precision,
             "l2": "inputs larger than L2 (no flush)"}
+
+
+def make_workload(pkg, name, scale):
+    idx = {"cfg1": 1, "cfg2": 2, "cfg3": 3, "cfg5": 5}[name]
+    return pkg.mesh.config_system(idx, scale=scale)
+
+
+def device_solves(pkg, topo, val, b, x, method, prec, tol, opts, steps, warmup, barrier=None):
+    """Warm-up, then `steps` timed solves with CUDA events on the current
+    stream; returns (elapsed seconds, list of result records)."""
+    import torch
+    for _ in range(warmup):
+        x.zero_()
+        res = topo.solve(val, b, x, method, prec, 20000, tol, opts=opts)
+        if res["status"] != pkg.OK:
+            raise RuntimeError(f"solve failed: {res}")
+    if barrier:
+        barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = []
+    e0.record()
+    for _ in range(steps):
+        x.zero_()
+        out.append(topo.solve(val, b, x, method, prec, 20000, tol, opts=opts))
+    e1.record()
+    torch.cuda.synchronize()
+    if barrier:
+        barrier()
+    return e0.elapsed_time(e1) * 1e-3, out
+
+
+def mixed_vs_fp64(pkg, dev, scale, prec, reps):
+    """The variable-density pressure system (cfg3): CG with the given
+    preconditioner in FP64 (reference arithmetic) and in mixed precision
+    (FP32 inner solves, FP64 refinement), same absolute tolerance."""
+    import numpy as np
+    import torch
+    s = make_workload(pkg, "cfg3", scale)
+    topo = pkg.Topology.from_system(s)
+    val = torch.from_numpy(s.A[:-1].copy()).to(dev)
+    b = torch.from_numpy(s.b.copy()).to(dev)
+    x = torch.zeros(s.N, dtype=torch.float64, device=dev)
+    res = {}
+    xs = {}
+    for mode, opts in (("fp64", pkg.options(precision=pkg.FP64)),
+                       ("mixed", pkg.options(precision=pkg.MIXED))):
+        el, out = device_solves(pkg, topo, val, b, x, "cg", prec, s.tol, opts, reps, 1)
+        r = out[-1]
+        res[mode] = {"ms": 1e3 * el / reps, "iterations": r["iterations"],
+                     "refinements": r["refinements"], "fin_res": r["fin_res"],
+                     "gbs": r["bytes"] / r["seconds"] / 1e9, "status": r["status"]}
+        xs[mode] = x.clone()
+    d = float((xs["mixed"] - xs["fp64"]).abs().max() / xs["fp64"].abs().max())
+    topo.close()
+    return {"workload": f"{s.name}, CG prec {prec}, tol 1e-8*||b|| absolute", "n": s.N,
+            "fp64": res["fp64"], "mixed": res["mixed"],
+            "speedup": res["fp64"]["ms"] / res["mixed"]["ms"],
+            "mixed_rel_diff_vs_fp64": d}
 
 
 def main():
@@ -185,7 +244,15 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
+    ap.add_argument("--scale", type=int, default=None, help="box edge (default: the config's)")
+    ap.add_argument("--method", default="bicg")
+    ap.add_argument("--prec", type=int, default=1)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--compare-scale", type=int, default=256,
+                    help="edge of the cfg3 mixed-vs-FP64 comparison (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -206,105 +273,101 @@ def main():
     pkg.load_library()
     peak, peak_kind = load_peaks()
 
-    s = pkg.mesh.config_system(2)
-    method, prec = "bicg", 1
+    s = make_workload(pkg, args.workload, args.scale)
+    method, prec = args.method, args.prec
     tol = s.tol
     dev = torch.device("cuda", local)
     topo = pkg.Topology.from_system(s)
     val = torch.from_numpy(s.A[:-1].copy()).to(dev)
     b = torch.from_numpy(s.b.copy()).to(dev)
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
-
-    def step():
-        x.zero_()
-        return topo.solve(val, b, x, method, prec, 200, tol)
+    opts = pkg.options(precision=pkg.MIXED if args.precision == "mixed" else pkg.FP64)
 
     def barrier():
         if world > 1:
             dist.barrier()
 
-    for _ in range(args.warmup):
-        res = step()
-    if res["status"] != pkg.OK:
-        raise RuntimeError(f"solve failed: {res}")
     clocks = ClockSampler(local)
-    barrier()
-    torch.cuda.synchronize()
     clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    kern_s, kern_b, iters = 0.0, 0.0, []
-    e0.record()
-    for _ in range(args.steps):
-        r = step()
-        kern_s += r["seconds"]
-        kern_b += r["bytes"]
-        iters.append(r["iterations"])
-    e1.record()
-    torch.cuda.synchronize()
-    barrier()
+    el, results = device_solves(pkg, topo, val, b, x, method, prec, tol, opts, args.steps,
+                                args.warmup, barrier)
     clk = clocks.stop()
-    el = e0.elapsed_time(e1) * 1e-3
     if world > 1:
         t = torch.tensor([el], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         el = float(t.item())
     value = world * args.steps / el
+    kern_s = sum(r["seconds"] for r in results)
+    kern_b = sum(r["bytes"] for r in results)
+    iters = [r["iterations"] for r in results]
 
-    # e2e through the Fortran-facing C ABI, inputs in pinned host memory.
-    A_h = torch.from_numpy(s.A.copy()).pin_memory().numpy()
-    x_h = torch.zeros(s.NB + s.N + 1, dtype=torch.float64).pin_memory().numpy()
-    r_h = torch.zeros(s.N, dtype=torch.float64).pin_memory().numpy()
-    pkg.set_options()
-    e2e_t = 0.0
-    for k in range(args.warmup + args.steps):
-        x_h[:] = 0.0
-        r_h[:] = s.b
-        t0 = time.perf_counter()
-        out = pkg.bicg(s.N, s.NB, s.NONZ, A_h, s.Acol, s.Arow, s.Adia, s.Ab, x_h, r_h, prec, 200,
-                       tol)
-        t1 = time.perf_counter()
-        if k >= args.warmup:
-            e2e_t += t1 - t0
-    if out.status != pkg.OK:
-        raise RuntimeError(f"e2e solve failed: {out}")
-    if world > 1:
-        t = torch.tensor([e2e_t], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_t = float(t.item())
-    e2e = world * args.steps / e2e_t
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic", "config": workload_config(s, method, prec, args.precision),
+        "iterations": int(statistics.median(iters)),
+        "time_to_tol_ms": 1e3 * el / args.steps,
+    }
+    achieved = kern_b / kern_s / 1e9
+    line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "kernel": ("mixed_kernel" if args.precision == "mixed" else
+                                   "krylov_kernel<double>") + " (one persistent launch per solve)",
+                        "peak_kind": peak_kind}
+
+    if not args.no_e2e:
+        # e2e through the Fortran-facing C ABI, inputs in pinned host memory.
+        A_h = torch.from_numpy(s.A.copy()).pin_memory().numpy()
+        x_h = torch.zeros(s.NB + s.N + 1, dtype=torch.float64).pin_memory().numpy()
+        r_h = torch.zeros(s.N, dtype=torch.float64).pin_memory().numpy()
+        pkg.set_options(precision=pkg.MIXED if args.precision == "mixed" else pkg.FP64)
+        legacy = {"cg": pkg.cg, "bicg": pkg.bicg, "cgs": pkg.cgs}[method]
+        e2e_t = 0.0
+        for k in range(args.warmup + args.steps):
+            x_h[:] = 0.0
+            r_h[:] = s.b
+            t0 = time.perf_counter()
+            out = legacy(s.N, s.NB, s.NONZ, A_h, s.Acol, s.Arow, s.Adia, s.Ab, x_h, r_h, prec,
+                         20000, tol)
+            t1 = time.perf_counter()
+            if k >= args.warmup:
+                e2e_t += t1 - t0
+        pkg.set_options()
+        if out.status != pkg.OK:
+            raise RuntimeError(f"e2e solve failed: {out}")
+        if world > 1:
+            t = torch.tensor([e2e_t], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_t = float(t.item())
+        line["e2e"] = {"value": world * args.steps / e2e_t, "unit": "solves/s",
+                       "h2d_bytes_per_step": int(8 * s.nnz + 16 * s.N),
+                       "d2h_bytes_per_step": int(16 * s.N)}
 
     # standalone SELL products (FP64 and FP32) for the SpMV roofline
     y = torch.empty_like(x)
     xs = torch.rand(s.N, dtype=torch.float64, device=dev)
-    spmv64 = topo.spmv(val, xs, y, repeat=20)
     sl = (s.N + 31) // 32
-    b64 = s.nnz * 12.0 + 8.0 * (sl + 1) + 16.0 * s.N
+    for tag, fp32, sv in (("spmv_fp64", False, 8), ("spmv_fp32", True, 4)):
+        sec = topo.spmv(val, xs, y, repeat=20, fp32=fp32)
+        byts = s.nnz * (sv + 4.0) + 8.0 * (sl + 1) + 2.0 * s.N * sv
+        line[tag] = {"gbs": byts / sec / 1e9, "frac": byts / sec / 1e9 / peak, "us": sec * 1e6,
+                     "bytes": byts}
+    line["clocks"] = clk
+    line["gpu_launches"] = 2 * args.steps
+    topo.close()
+    del val, b, x, y, xs
+    torch.cuda.empty_cache()
 
-    achieved = kern_b / kern_s / 1e9
-    line = {
-        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": workload_config(s, method, prec),
-        "iterations": int(statistics.median(iters)),
-        "time_to_tol_ms": 1e3 * el / args.steps,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "krylov_kernel<double> (persistent BiCG/CG solve)",
-                     "peak_kind": peak_kind},
-        "spmv_fp64": {"gbs": b64 / spmv64 / 1e9, "frac": b64 / spmv64 / 1e9 / peak,
-                      "ms": spmv64 * 1e3},
-        "e2e": {"value": e2e, "unit": "solves/s",
-                "h2d_bytes_per_step": int(8 * s.nnz + 16 * s.N),
-                "d2h_bytes_per_step": int(16 * s.N)},
-        "clocks": clk,
-        "gpu_launches": 2 * args.steps,
-    }
+    if rank == 0 and args.compare_scale:
+        line["mixed_vs_fp64"] = mixed_vs_fp64(pkg, dev, args.compare_scale, 1, 1)
     if rank == 0 and not args.no_cpu_baseline:
         v, n, it, el_c = cpu_reference_throughput(s, method, prec, 1, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
-                                "sample": f"{n} full BiCG solves ({it} iterations) of the same "
-                                          f"system, oracle C restatement, 1 thread, {el_c:.1f} s"}
+                                "sample": f"{n} full {method} solves ({it} iterations) of the "
+                                          f"same system, oracle C restatement, 1 thread, "
+                                          f"{el_c:.1f} s"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

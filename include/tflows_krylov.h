@@ -51,9 +51,14 @@ extern "C" {
 typedef struct tflows_options {
     int precision;       /* TFLOWS_FP64 (default) or TFLOWS_MIXED            */
     int tol_mode;        /* TFLOWS_TOL_ABSOLUTE (default) or _RELATIVE       */
-    double inner_rtol;   /* mixed: inner residual reduction per refinement   */
-    int inner_maxiter;   /* mixed: inner iteration cap per refinement        */
-    int max_refinements; /* mixed: outer FP64 refinement steps cap          */
+    double inner_rtol;   /* mixed: FP32 residual reduction between FP64
+                            refinements (default 1e-1)                      */
+    int inner_maxiter;   /* mixed, restarted: inner iterations per step     */
+    int max_refinements; /* mixed, restarted: refinement steps cap          */
+    int refine_restart;  /* mixed: 1 = restart the inner solve at each FP64
+                            refinement (default, always for CGS); 0 = CG keeps
+                            its search direction across refinements
+                            (reliable updates)                              */
     int ic_sweeps;       /* mixed + prec 2: 0 = exact triangular sweeps,
                             k > 0 = k Jacobi sweeps per triangle            */
     int ic_bf16;         /* mixed + prec 2: IC off-diagonals stored in BF16 */

@@ -60,7 +60,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
         def compile_one(src):
             obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-            cmd = [cc, *ARCH, *NVCC_FLAGS, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+            extra = os.environ.get("TFLOWS_NVCC_EXTRA", "").split()
+            cmd = [cc, *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src),
+                   "-o", obj]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise NativeLibraryError(f"nvcc failed for {src}:\n{r.stderr}")
@@ -87,7 +89,8 @@ _VP = ctypes.c_void_p
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("tol_mode", ctypes.c_int),
                 ("inner_rtol", ctypes.c_double), ("inner_maxiter", ctypes.c_int),
-                ("max_refinements", ctypes.c_int), ("ic_sweeps", ctypes.c_int),
+                ("max_refinements", ctypes.c_int), ("refine_restart", ctypes.c_int),
+                ("ic_sweeps", ctypes.c_int),
                 ("ic_bf16", ctypes.c_int), ("timeout_s", ctypes.c_double),
                 ("block_size", ctypes.c_int), ("grid_blocks", ctypes.c_int),
                 ("device", ctypes.c_int)]
@@ -152,7 +155,7 @@ def load(path: str | None = None):
     with _lock:
         if _lib is not None:
             return _lib
-    p = path or LIB_PATH
+    p = path or os.environ.get("TFLOWS_LIB") or LIB_PATH
     if not os.path.exists(p):
         build()
     try:

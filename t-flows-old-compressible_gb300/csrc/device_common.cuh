@@ -131,7 +131,9 @@ __device__ __forceinline__ bool wait_cell(const T* p, T& out, DevCtl* ctl, long 
     long long t0 = globaltimer_ns();
     unsigned spins = 0;
     while (true) {
-        __nanosleep(40);
+        // exponential back-off 32 -> 512 ns keeps many waiting threads from
+        // flooding L2 with polls
+        __nanosleep(32u << (spins < 4u ? spins : 4u));
         b = C::load(p);
         if (b != C::kSentinel) {
             out = C::value(b);
@@ -186,7 +188,52 @@ struct Grid {
     int wg;   // global warp index
     int nw;   // warps in the grid
     int lane;
+    int tid;  // global thread index
+    int nt;   // threads in the grid
+    unsigned ep_f;  // forward / backward level-sweep epochs (counter targets)
+    unsigned ep_b;
 };
+
+__device__ __forceinline__ void grid_init(Grid& g, DevCtl* ctl, double* partials,
+                                          long long timeout_ns) {
+    g.ctl = ctl;
+    g.partials = partials;
+    g.timeout_ns = timeout_ns;
+    g.target = 0;
+    g.nblocks = gridDim.x;
+    g.lane = threadIdx.x & 31;
+    g.tid = blockIdx.x * blockDim.x + threadIdx.x;
+    g.nt = gridDim.x * blockDim.x;
+    g.wg = g.tid >> 5;
+    g.nw = g.nt >> 5;
+    g.ep_f = 0;
+    g.ep_b = 0;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Wait (one thread) until *p >= target; bounded like every other wait.
+__device__ __forceinline__ bool wait_count(const unsigned* p, unsigned target, DevCtl* ctl,
+                                           long long timeout_ns, int where) {
+    if (ld_acquire_u32(p) >= target) return true;
+    long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    while (true) {
+        __nanosleep(32);
+        if (ld_acquire_u32(p) >= target) return true;
+        if ((++spins & 127u) == 0u) {
+            if (ld_relaxed_s32(&ctl->abort)) return false;
+            if (globaltimer_ns() - t0 > timeout_ns) {
+                raise_abort(ctl, ST_TIMEOUT, where);
+                return false;
+            }
+        }
+    }
+}
 
 // Grid-wide barrier with release/acquire ordering (every write before the
 // barrier is visible to every read after it).  Returns false when the

@@ -30,6 +30,11 @@ struct DeviceTopology {
     int* meta = nullptr;       // n: length | diag slot << 16
     int* perm_f = nullptr;
     int* perm_b = nullptr;
+    int* chunk_lev_f = nullptr;  // level of each 32-row chunk of perm_f
+    int* chunk_lev_b = nullptr;
+    int* lev_nch_f = nullptr;    // chunks per level
+    int* lev_nch_b = nullptr;
+    unsigned* lev_cnt = nullptr; // completion counters: nlev_f forward, then nlev_b
     int* tpos = nullptr;       // transpose map (lazy)
     // host copies (0-based) for lazy derived data
     std::vector<int> h_rowptr, h_col, h_diag;
@@ -66,6 +71,7 @@ struct SolveRequest {
     int inner_maxiter = 1000;
     int max_refinements = 30;
     int ic_sweeps = 0;
+    int refine_restart = 0;
     double timeout_s = 5.0;
     int block = 0;
     int grid = 0;

@@ -11,6 +11,12 @@ namespace tflows {
 namespace {
 
 constexpr int kBlock = 256;
+// Resident blocks per SM the persistent kernels are compiled for (register
+// budget 65536 / (kBlock * kMinBlocks) per thread).
+#ifndef TFLOWS_MINBLOCKS
+#define TFLOWS_MINBLOCKS 4
+#endif
+constexpr int kMinBlocks = TFLOWS_MINBLOCKS;
 
 template <typename T>
 struct KParams {
@@ -34,27 +40,21 @@ __device__ int status_of(const SolveOut& o, const DevCtl* ctl) {
     }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kBlock) krylov_kernel(KParams<T> P) {
+// METHOD: 0 CG (and BiCG), 2 CGS, 9 Prec1 only.
+template <typename T, int METHOD>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) krylov_kernel(KParams<T> P) {
     Grid g;
-    g.ctl = P.ctl;
-    g.partials = P.partials;
-    g.timeout_ns = P.timeout_ns;
-    g.target = 0;
-    g.nblocks = gridDim.x;
-    g.lane = threadIdx.x & 31;
-    g.wg = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    g.nw = (int)((gridDim.x * blockDim.x) >> 5);
+    grid_init(g, P.ctl, P.partials, P.timeout_ns);
     SolveOut out;
     out.exit_kind = 0;
     out.iterations = 0;
     out.ini_res = 0.0;
     out.fin_res = 0.0;
     out.bnrm2 = 0.0;
-    if (P.mode == 1) {
+    if (METHOD == 9) {
         bool ok = prec1_phase(g, P.m, P.v.D, P.cfg.prec);
         out.exit_kind = ok ? EXIT_CONVERGED : EXIT_ABORT;
-    } else if (P.cfg.method == 2) {
+    } else if (METHOD == 2) {
         cgs_solve(g, P.m, P.v, P.cfg, out);
     } else {
         cg_solve(g, P.m, P.v, P.cfg, out);
@@ -64,6 +64,56 @@ __global__ void __launch_bounds__(kBlock) krylov_kernel(KParams<T> P) {
         s->status = status_of(out, P.ctl);
         s->exit_kind = out.exit_kind;
         s->iterations = out.iterations;
+        s->ini_res = out.ini_res;
+        s->fin_res = out.fin_res;
+        s->bnrm2 = out.bnrm2;
+        s->timeout_where = P.ctl->where;
+    }
+}
+
+struct MixedParams {
+    Mat<double> m64;
+    Mat<float> m32;
+    double* x64;
+    double* r64;
+    const double* b64;
+    double* D64;
+    double* xbest;
+    Vecs<float> v32;
+    MixedCfg cfg;
+    DevCtl* ctl;
+    DevState* state;
+    double* partials;
+    long long timeout_ns;
+};
+
+// KIND: 0 restarted CG, 2 restarted CGS, 1 CG with reliable updates.
+template <int KIND>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) mixed_kernel(MixedParams P) {
+    Grid g;
+    grid_init(g, P.ctl, P.partials, P.timeout_ns);
+    MixedOut out;
+    out.exit_kind = 0;
+    out.iterations = 0;
+    out.refinements = 0;
+    out.ini_res = 0.0;
+    out.fin_res = 0.0;
+    out.bnrm2 = 0.0;
+    if (KIND == 1)
+        mixed_cg_reliable(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.xbest, P.v32, P.cfg,
+                          out);
+    else
+        mixed_solve(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.v32, P.cfg, out);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        DevState* s = P.state;
+        SolveOut o;
+        o.exit_kind = out.exit_kind;
+        o.fin_res = out.fin_res;
+        s->status = status_of(o, P.ctl);
+        s->exit_kind = out.exit_kind;
+        s->iterations = out.iterations;
+        s->inner_iters = out.iterations;
+        s->refinements = out.refinements;
         s->ini_res = out.ini_res;
         s->fin_res = out.fin_res;
         s->bnrm2 = out.bnrm2;
@@ -84,6 +134,15 @@ __global__ void fill_sentinel_kernel(T* p, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
         p[i] = v;
+}
+
+__global__ void to_float_kernel(const double* __restrict__ a, float* __restrict__ b, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+__global__ void to_double_kernel(const float* __restrict__ a, double* __restrict__ b, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
 }
 
 // SELL values from stored-order values: one thread per row.
@@ -159,9 +218,20 @@ Mat<T> make_mat(const DeviceTopology& t, const T* sval) {
     m.meta = t.meta;
     m.perm_f = t.perm_f;
     m.perm_b = t.perm_b;
+    m.clev_f = t.chunk_lev_f;
+    m.clev_b = t.chunk_lev_b;
+    m.lnch_f = t.lev_nch_f;
+    m.lnch_b = t.lev_nch_b;
+    m.cnt_f = t.lev_cnt;
+    m.cnt_b = t.lev_cnt ? t.lev_cnt + t.nlev_f : nullptr;
     m.nchunk_f = t.nchunk_f;
     m.nchunk_b = t.nchunk_b;
     return m;
+}
+
+void reset_counters(const DeviceTopology& t, cudaStream_t s) {
+    if (t.lev_cnt)
+        cudaMemsetAsync(t.lev_cnt, 0, sizeof(unsigned) * (size_t)(t.nlev_f + t.nlev_b), s);
 }
 
 int blocks_for(int nslices) { return std::max(1, (nslices + kBlock / 32 - 1) / (kBlock / 32)); }
@@ -249,18 +319,17 @@ Vecs<T> carve(T* base, size_t cap, T* x, T* r) {
     return v;
 }
 
-template <typename T>
-int max_coresident(int block) {
+template <typename K>
+int max_coresident(K kernel, int block) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, krylov_kernel<T>, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
     return std::max(1, per_sm) * sms();
 }
 
-template <typename T>
-cudaError_t launch_persistent(KParams<T>& P, int grid, cudaStream_t s) {
-    void* args[] = {&P};
-    return cudaLaunchCooperativeKernel((const void*)krylov_kernel<T>, dim3(grid), dim3(kBlock), args,
-                                       0, s);
+template <typename K, typename P>
+cudaError_t launch_coop(K kernel, P& params, int grid, cudaStream_t s) {
+    void* args[] = {&params};
+    return cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(kBlock), args, 0, s);
 }
 
 int choose_grid(const DeviceTopology& t, int requested, int max_blocks) {
@@ -284,8 +353,10 @@ int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, doubl
     P.timeout_ns = (long long)(timeout_s * 1e9);
     P.mode = 1;
     cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
-    const int grid = choose_grid(t, 0, max_coresident<double>(kBlock));
-    cudaError_t e = launch_persistent(P, grid, s);
+    reset_counters(t, s);
+    auto kern = krylov_kernel<double, 9>;
+    const int grid = choose_grid(t, 0, max_coresident(kern, kBlock));
+    cudaError_t e = launch_coop(kern, P, grid, s);
     if (e != cudaSuccess) {
         rep.status = ST_CUDA_ERROR;
         rep.message = cudaGetErrorString(e);
@@ -303,8 +374,79 @@ int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, doubl
     return rep.status;
 }
 
+namespace {
+
+int run_mixed(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
+              cudaStream_t s, SolveReport& rep) {
+    MixedParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.m64 = make_mat<double>(t, ws.sval64);
+    P.m32 = make_mat<float>(t, ws.sval32);
+    P.x64 = x;
+    P.r64 = r;
+    // b is kept in the FP64 workspace slot 13 (the residual slot r is
+    // rewritten by every refinement).
+    double* b64 = ws.vec64 + 13 * ws.vec_cap;
+    cudaError_t e = cudaMemcpyAsync(b64, r, sizeof(double) * t.n, cudaMemcpyDeviceToDevice, s);
+    P.b64 = b64;
+    P.D64 = ws.vec64 + 4 * ws.vec_cap;
+    P.xbest = ws.vec64;
+    P.v32 = carve<float>(ws.vec32, ws.vec_cap, ws.vec32 + 11 * ws.vec_cap, ws.vec32 + 12 * ws.vec_cap);
+    P.cfg.method = rq.method == 2 ? 2 : 0;
+    P.cfg.prec = rq.prec;
+    P.cfg.max_ref = rq.max_refinements > 0 ? rq.max_refinements : 30;
+    P.cfg.inner_maxiter = rq.inner_maxiter > 0 ? rq.inner_maxiter : 2000;
+    P.cfg.maxiter = std::max(rq.maxiter, 0);
+    P.cfg.restart = rq.refine_restart;
+    P.cfg.tol = rq.tol;
+    P.cfg.inner_rtol = rq.inner_rtol > 0 ? rq.inner_rtol : 1e-1;
+    P.cfg.tol_is_relative = rq.tol_relative;
+    P.cfg.x_is_zero = rq.x_is_zero;
+    P.ctl = (DevCtl*)ws.ctl;
+    P.state = (DevState*)ws.state;
+    P.partials = ws.partials;
+    P.timeout_ns = (long long)(rq.timeout_s * 1e9);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
+    reset_counters(t, s);
+    auto kern = P.cfg.method == 2 ? mixed_kernel<2> : (P.cfg.restart ? mixed_kernel<0> : mixed_kernel<1>);
+    const int grid = choose_grid(t, rq.grid, max_coresident(kern, kBlock));
+    cudaEventRecord(ws.ev0, s);
+    if (e == cudaSuccess) e = launch_coop(kern, P, grid, s);
+    cudaEventRecord(ws.ev1, s);
+    DevState st;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ws.state, sizeof(st), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        rep.status = ST_CUDA_ERROR;
+        rep.message = std::string("mixed solver: ") + cudaGetErrorString(e);
+        return rep.status;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ws.ev0, ws.ev1);
+    rep.status = st.status;
+    rep.exit_kind = st.exit_kind;
+    rep.iterations = st.iterations;
+    rep.inner_iterations = st.inner_iters;
+    rep.refinements = st.refinements;
+    rep.ini_res = st.ini_res;
+    rep.fin_res = st.fin_res;
+    rep.seconds = ms * 1e-3;
+    const double sl = 8.0 * (t.nslices + 1);
+    const double spmv32 = (double)t.nnz * 8.0 + sl + 8.0 * t.n;
+    const double spmv64 = (double)t.nnz * 12.0 + sl + 16.0 * t.n;
+    const double inner_it = P.cfg.method == 2 ? 2 * spmv32 + 4.0 * t.n * 22
+                                              : spmv32 + 4.0 * t.n * (rq.prec == 1 ? 12 : 10);
+    rep.bytes = inner_it * st.inner_iters + (spmv64 + 8.0 * t.n * 4) * (st.refinements + 1);
+    if (st.status == ST_TIMEOUT)
+        rep.message = "device wait exceeded the timeout (site " + std::to_string(st.timeout_where) + ")";
+    return rep.status;
+}
+
+}  // namespace
+
 int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
               cudaStream_t s, SolveReport& rep) {
+    if (rq.precision == 1) return run_mixed(t, ws, rq, x, r, s, rep);
     KParams<double> P;
     std::memset(&P, 0, sizeof(P));
     P.m = make_mat<double>(t, ws.sval64);
@@ -322,14 +464,15 @@ int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, do
     P.timeout_ns = (long long)(rq.timeout_s * 1e9);
     P.mode = 0;
     cudaError_t e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
+    reset_counters(t, s);
     if (rq.prec == 2) {
         const long long nvec = (long long)t.nslices * kWarp;
         fill_sentinel_kernel<double><<<std::min(1024, (int)((nvec + 255) / 256)), 256, 0, s>>>(P.v.w, nvec);
     }
-    const int maxb = max_coresident<double>(kBlock);
-    const int grid = choose_grid(t, rq.grid, maxb);
+    auto kern = P.cfg.method == 2 ? krylov_kernel<double, 2> : krylov_kernel<double, 0>;
+    const int grid = choose_grid(t, rq.grid, max_coresident(kern, kBlock));
     cudaEventRecord(ws.ev0, s);
-    if (e == cudaSuccess) e = launch_persistent(P, grid, s);
+    if (e == cudaSuccess) e = launch_coop(kern, P, grid, s);
     cudaEventRecord(ws.ev1, s);
     if (e != cudaSuccess) {
         rep.status = ST_CUDA_ERROR;
@@ -376,24 +519,26 @@ cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, d
 cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, double* y, bool fp32,
                      int repeat, cudaStream_t s, float* ms) {
     const int nb = std::min(blocks_for(t.nslices), sms() * 8);
+    float* x32 = ws.vec32;
+    float* y32 = ws.vec32 + ws.vec_cap;
+    if (fp32) {
+        to_float_kernel<<<std::min(1024, (t.n + 255) / 256), 256, 0, s>>>(x, x32, t.n);
+    }
     cudaEventRecord(ws.ev0, s);
     for (int k = 0; k < std::max(1, repeat); ++k) {
         if (fp32) {
-            float* x32 = ws.vec32;
-            float* y32 = ws.vec32 + ws.vec_cap;
-            if (k == 0) {
-                // conversion outside the timed product is done by the caller
-            }
             spmv_kernel<float, float><<<nb, kBlock, 0, s>>>(make_mat<float>(t, ws.sval32), x32, y32);
         } else {
             spmv_kernel<double, double><<<nb, kBlock, 0, s>>>(make_mat<double>(t, ws.sval64), x, y);
         }
     }
     cudaEventRecord(ws.ev1, s);
+    if (fp32) to_double_kernel<<<std::min(1024, (t.n + 255) / 256), 256, 0, s>>>(y32, y, t.n);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = cudaEventSynchronize(ws.ev1);
     if (ms) cudaEventElapsedTime(ms, ws.ev0, ws.ev1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     return e;
 }
 

@@ -44,6 +44,12 @@ struct Mat {
     const int* __restrict__ meta;        // per row: length | diag slot << 16
     const int* __restrict__ perm_f;      // forward level order, 32-padded, -1 pads
     const int* __restrict__ perm_b;      // backward level order
+    const int* __restrict__ clev_f;      // level of each 32-row chunk
+    const int* __restrict__ clev_b;
+    const int* __restrict__ lnch_f;      // chunks per level
+    const int* __restrict__ lnch_b;
+    unsigned* cnt_f;                     // per-level completion counters
+    unsigned* cnt_b;
     int nchunk_f;
     int nchunk_b;
 };
@@ -83,12 +89,58 @@ struct SolveOut {
     double bnrm2;
 };
 
+// Rows in SELL order: row i = 32*slice + lane (used by the matrix phases).
 #define TF_FOR_ROWS(g, m, i)                                        \
     for (int s__ = (g).wg; s__ < (m).nslices; s__ += (g).nw)        \
         for (int i = s__ * kWarp + (g).lane, once__ = 1; once__; once__ = 0) \
             if (i < (m).n)
 
-// q_i = sum_j a_ij x_j over row i = 32*s + lane, left to right from 0.
+// Four consecutive rows per thread with 16-byte vector accesses (the vector
+// phases).  Every work vector is padded to a multiple of 32 elements, so the
+// group i..i+3 is in bounds; contributions of rows >= n are masked.
+#define TF_FOR4(g, m, i) for (int i = 4 * (g).tid; i < (m).n; i += 4 * (g).nt)
+
+template <typename T>
+struct V4 {
+    T a[4];
+};
+__device__ __forceinline__ V4<float> ld4(const float* p) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    return {{v.x, v.y, v.z, v.w}};
+}
+__device__ __forceinline__ void st4(float* p, const V4<float>& v) {
+    *reinterpret_cast<float4*>(p) = make_float4(v.a[0], v.a[1], v.a[2], v.a[3]);
+}
+__device__ __forceinline__ V4<double> ld4(const double* p) {
+    const double2 u = reinterpret_cast<const double2*>(p)[0];
+    const double2 w = reinterpret_cast<const double2*>(p)[1];
+    return {{u.x, u.y, w.x, w.y}};
+}
+__device__ __forceinline__ void st4(double* p, const V4<double>& v) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(v.a[0], v.a[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v.a[2], v.a[3]);
+}
+
+// Dot-product partials accumulate per thread in the working precision (FP64
+// sums in FP64 mode; FP32 sums in the FP32 inner solves, where a per-element
+// FP64 accumulation would load GB300's narrow FP64 pipe) and are combined
+// across threads and blocks in FP64.
+template <int K, typename T>
+__device__ __forceinline__ void publish_t(Grid& g, int slot, const T (&v)[K]) {
+    double d[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) d[k] = (double)v[k];
+    publish<K>(g, slot, d);
+}
+
+// Jacobi step z = r / D.  FP64 keeps the reference's correctly rounded
+// division; the FP32 inner solves hold 1/D and multiply.
+__device__ __forceinline__ double jacobi(double r, double d) { return r / d; }
+__device__ __forceinline__ float jacobi(float r, float dinv) { return r * dinv; }
+
+// q_i = sum_j a_ij x_j over row i = 32*s + lane, left to right from 0.  Rows
+// of at most 8 stored entries (every hex or prism cell) take a fully
+// unrolled path: all index and value loads issue before the gathers.
 template <typename T, typename X>
 __device__ __forceinline__ T sell_row(const Mat<T>& m, int s, int lane, const X* __restrict__ xv) {
     const long long b0 = m.soff[s];
@@ -96,27 +148,24 @@ __device__ __forceinline__ T sell_row(const Mat<T>& m, int s, int lane, const X*
     const int* cp = m.scol + b0 + lane;
     const T* vp = m.sval + b0 + lane;
     T acc = T(0);
-    int t = 0;
-    for (; t + 4 <= w; t += 4) {
-        const int c0 = cp[0], c1 = cp[32], c2 = cp[64], c3 = cp[96];
-        const T v0 = vp[0], v1 = vp[32], v2 = vp[64], v3 = vp[96];
-        const T x0 = c0 >= 0 ? T(xv[c0]) : T(0);
-        const T x1 = c1 >= 0 ? T(xv[c1]) : T(0);
-        const T x2 = c2 >= 0 ? T(xv[c2]) : T(0);
-        const T x3 = c3 >= 0 ? T(xv[c3]) : T(0);
-        if (c0 >= 0) acc = acc + v0 * x0;
-        if (c1 >= 0) acc = acc + v1 * x1;
-        if (c2 >= 0) acc = acc + v2 * x2;
-        if (c3 >= 0) acc = acc + v3 * x3;
-        cp += 128;
-        vp += 128;
+    if (w <= 8) {
+        int c[8];
+        T v[8], xx[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            c[t] = t < w ? cp[32 * t] : -1;
+            v[t] = t < w ? vp[32 * t] : T(0);
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) xx[t] = c[t] >= 0 ? T(xv[c[t]]) : T(0);
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (c[t] >= 0) acc = acc + v[t] * xx[t];
+        return acc;
     }
-    for (; t < w; ++t) {
-        const int c = cp[0];
-        const T v = vp[0];
-        if (c >= 0) acc = acc + v * T(xv[c]);
-        cp += 32;
-        vp += 32;
+    for (int t = 0; t < w; ++t) {
+        const int c = cp[32 * t];
+        if (c >= 0) acc = acc + vp[32 * t] * T(xv[c]);
     }
     return acc;
 }
@@ -129,6 +178,21 @@ __device__ __forceinline__ T sell_resid_row(const Mat<T>& m, int s, int lane, T 
     const int w = (int)((m.soff[s + 1] - b0) >> 5);
     const int* cp = m.scol + b0 + lane;
     const T* vp = m.sval + b0 + lane;
+    if (w <= 8) {
+        int c[8];
+        T v[8], xx[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            c[t] = t < w ? cp[32 * t] : -1;
+            v[t] = t < w ? vp[32 * t] : T(0);
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) xx[t] = c[t] >= 0 ? T(xv[c[t]]) : T(0);
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (c[t] >= 0) ri = ri - v[t] * xx[t];
+        return ri;
+    }
     for (int t = 0; t < w; ++t) {
         const int c = cp[32 * t];
         if (c >= 0) ri = ri - vp[32 * t] * T(xv[c]);
@@ -142,33 +206,138 @@ __device__ __forceinline__ T diag_value(const Mat<T>& m, int i) {
     return m.sval[m.soff[i >> 5] + (i & 31) + 32LL * dslot];
 }
 
+// ---- sync-free level-ordered sweeps ----------------------------------------
+// Rows are visited in wavefront-level order in chunks of 32 rows of one
+// level (levels padded to whole warps); warp w takes chunks w, w+nw, ... in
+// increasing order.  A row waits only for the specific earlier rows it reads,
+// through their value-as-flag cells; every index, coefficient and own-row
+// operand is loaded before the first wait, so a row's critical path is one
+// cell load per dependency.  A chunk only ever waits on rows of lower levels,
+// which sit in chunks of lower index, so with all warps resident the sweep
+// cannot deadlock.
+constexpr int kSweepMax = 8;  // dependencies prefetched per row
+// Pause between polls of not-yet-ready cells, in ns (0: poll back to back).
+#ifndef TFLOWS_SWEEP_SLEEP
+#define TFLOWS_SWEEP_SLEEP 0
+#endif
+
+// Wait for up to kSweepMax cells at once: all not-yet-ready cells are
+// re-polled together after each short sleep, so a row pays one round trip
+// after its last dependency lands instead of one per dependency.
+template <typename T>
+__device__ __forceinline__ bool wait_cells(const T* cells, const int (&c)[kSweepMax], int n,
+                                           T (&v)[kSweepMax], const Grid& g, int where) {
+    using C = Cell<T>;
+    unsigned pending = 0;
+#pragma unroll
+    for (int u = 0; u < kSweepMax; ++u) {
+        if (u < n) {
+            const auto b = C::load(cells + c[u]);
+            if (b == C::kSentinel) pending |= 1u << u;
+            else v[u] = C::value(b);
+        }
+    }
+    if (!pending) return true;
+    const long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    while (pending) {
+        if (TFLOWS_SWEEP_SLEEP > 0) __nanosleep(TFLOWS_SWEEP_SLEEP);
+#pragma unroll
+        for (int u = 0; u < kSweepMax; ++u) {
+            if (pending & (1u << u)) {
+                const auto b = C::load(cells + c[u]);
+                if (b != C::kSentinel) {
+                    v[u] = C::value(b);
+                    pending &= ~(1u << u);
+                }
+            }
+        }
+        if ((++spins & 63u) == 0u && pending) {
+            if (ld_relaxed_s32(&g.ctl->abort)) return false;
+            if (globaltimer_ns() - t0 > g.timeout_ns) {
+                raise_abort(g.ctl, ST_TIMEOUT, where);
+                return false;
+            }
+        }
+    }
+    return true;
+}
+
+// Forward-type row: acc - sum_{t in [t0,t1)} a_t * cell[col_t], summed in
+// slot order (the reference's order) once every cell has its value.
+template <typename T>
+__device__ __forceinline__ bool sweep_row(const Grid& g, const Mat<T>& m, long long base, int t0,
+                                          int t1, T acc, const T* cells, int where, T& out) {
+    const int n = t1 - t0;
+    if (n <= kSweepMax) {
+        int c[kSweepMax];
+        T a[kSweepMax], v[kSweepMax];
+#pragma unroll
+        for (int u = 0; u < kSweepMax; ++u) {
+            c[u] = u < n ? m.scol[base + 32LL * (t0 + u)] : 0;
+            a[u] = u < n ? m.sval[base + 32LL * (t0 + u)] : T(0);
+            v[u] = T(0);
+        }
+        if (!wait_cells(cells, c, n, v, g, where)) return false;
+#pragma unroll
+        for (int u = 0; u < kSweepMax; ++u)
+            if (u < n) acc = acc - a[u] * v[u];
+    } else {
+        for (int t = t0; t < t1; ++t) {
+            const int k = m.scol[base + 32LL * t];
+            const T av = m.sval[base + 32LL * t];
+            T v;
+            if (!wait_cell(cells + k, v, g.ctl, g.timeout_ns, where)) return false;
+            acc = acc - av * v;
+        }
+    }
+    out = acc;
+    return true;
+}
+
 // ---- Prec1 -----------------------------------------------------------------
 // prec 1: D_i = a_ii; prec 2: D_i = 1 / (a_ii - sum_{k<i} D_k a_ik a_ik);
-// otherwise D_i = 1 (Process/Prec1.f90:45-67).  Ends with a grid barrier.
+// otherwise D_i = 1 (Process/Prec1.f90:45-67).  IC ends with a grid barrier.
 template <typename T>
 __device__ bool prec1_phase(Grid& g, const Mat<T>& m, T* D, int prec) {
     if (prec == 2) {
         TF_FOR_ROWS(g, m, i) { D[i] = Cell<T>::sentinel(); }
         if (!grid_sync(g, 10)) return false;
         bool ok = true;
-        for (int c = g.wg; c < m.nchunk_f && ok; c += g.nw) {
-            const int row = m.perm_f[c * kWarp + g.lane];
+        for (int ch = g.wg; ch < m.nchunk_f && ok; ch += g.nw) {
+            const int row = m.perm_f[ch * kWarp + g.lane];
             if (row >= 0) {
-                const int meta = m.meta[row];
-                const int dslot = meta >> 16;
+                const int dslot = m.meta[row] >> 16;
                 const long long base = m.soff[row >> 5] + (row & 31);
                 T sum = m.sval[base + 32LL * dslot];
-                for (int t = 0; t < dslot && ok; ++t) {
-                    const int k = m.scol[base + 32LL * t];
-                    const T a = m.sval[base + 32LL * t];
-                    T dk;
-                    ok = wait_cell(D + k, dk, g.ctl, g.timeout_ns, 11);
-                    sum = sum - dk * a * a;
+                int c[kSweepMax];
+                T a[kSweepMax];
+                if (dslot <= kSweepMax) {
+                    T dv[kSweepMax];
+#pragma unroll
+                    for (int u = 0; u < kSweepMax; ++u) {
+                        c[u] = u < dslot ? m.scol[base + 32LL * u] : 0;
+                        a[u] = u < dslot ? m.sval[base + 32LL * u] : T(0);
+                        dv[u] = T(0);
+                    }
+                    ok = wait_cells(D, c, dslot, dv, g, 11);
+#pragma unroll
+                    for (int u = 0; u < kSweepMax; ++u)
+                        if (u < dslot) sum = sum - dv[u] * a[u] * a[u];
+                } else {
+                    for (int t = 0; t < dslot && ok; ++t) {
+                        const int k = m.scol[base + 32LL * t];
+                        const T av = m.sval[base + 32LL * t];
+                        T dk;
+                        ok = wait_cell(D + k, dk, g.ctl, g.timeout_ns, 11);
+                        sum = sum - dk * av * av;
+                    }
                 }
                 Cell<T>::store(D + row, T(1) / sum);
             }
         }
-        return grid_sync(g, 12);
+        const bool synced = grid_sync(g, 12);
+        return ok && synced;
     }
     TF_FOR_ROWS(g, m, i) { D[i] = (prec == 1) ? diag_value(m, i) : T(1); }
     return true;  // made visible by the caller's next barrier
@@ -183,43 +352,34 @@ __device__ bool prec1_phase(Grid& g, const Mat<T>& m, T* D, int prec) {
 template <typename T, typename Epi>
 __device__ bool ic_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* w, T* z, Epi epi) {
     bool ok = true;
-    for (int c = g.wg; c < m.nchunk_f && ok; c += g.nw) {
-        const int row = m.perm_f[c * kWarp + g.lane];
+    for (int ch = g.wg; ch < m.nchunk_f && ok; ch += g.nw) {
+        const int row = m.perm_f[ch * kWarp + g.lane];
         if (row >= 0) {
             const int dslot = m.meta[row] >> 16;
             const long long base = m.soff[row >> 5] + (row & 31);
-            T sum = rhs[row];
-            for (int t = 0; t < dslot && ok; ++t) {
-                const int k = m.scol[base + 32LL * t];
-                const T a = m.sval[base + 32LL * t];
-                T wk;
-                ok = wait_cell(w + k, wk, g.ctl, g.timeout_ns, 20);
-                sum = sum - a * wk;
-            }
-            Cell<T>::store(w + row, sum * D[row]);
+            const T d = D[row];
+            T sum;
+            ok = sweep_row(g, m, base, 0, dslot, rhs[row], w, 20, sum);
+            if (ok) Cell<T>::store(w + row, sum * d);
             z[row] = Cell<T>::sentinel();
         }
     }
-    if (!grid_sync(g, 21)) return false;
-    for (int c = g.wg; c < m.nchunk_b && ok; c += g.nw) {
-        const int row = m.perm_b[c * kWarp + g.lane];
+    if (!grid_sync(g, 21) || !ok) return false;
+    for (int ch = g.wg; ch < m.nchunk_b && ok; ch += g.nw) {
+        const int row = m.perm_b[ch * kWarp + g.lane];
         if (row >= 0) {
             const int meta = m.meta[row];
             const int len = meta & 0xFFFF, dslot = meta >> 16;
             const long long base = m.soff[row >> 5] + (row & 31);
             const T d = D[row];
-            T sum = w[row] / (d + T(kTiny));
-            for (int t = dslot + 1; t < len && ok; ++t) {
-                const int k = m.scol[base + 32LL * t];
-                const T a = m.sval[base + 32LL * t];
-                T zk;
-                ok = wait_cell(z + k, zk, g.ctl, g.timeout_ns, 22);
-                sum = sum - a * zk;
+            T sum;
+            ok = sweep_row(g, m, base, dslot + 1, len, w[row] / (d + T(kTiny)), z, 22, sum);
+            if (ok) {
+                const T zi = sum * d;
+                Cell<T>::store(z + row, zi);
+                w[row] = Cell<T>::sentinel();
+                epi(row, zi);
             }
-            const T zi = sum * d;
-            Cell<T>::store(z + row, zi);
-            w[row] = Cell<T>::sentinel();
-            epi(row, zi);
         }
     }
     return ok;
@@ -239,12 +399,14 @@ __device__ bool prologue(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         out.exit_kind = EXIT_ABORT;
         return false;
     }
-    double acc[1] = {0.0};
-    TF_FOR_ROWS(g, m, i) {
-        const double ri = v.r[i];
-        acc[0] += ri * ri;
+    T acc[1] = {T(0)};
+    TF_FOR4(g, m, i) {
+        const V4<T> r = ld4(v.r + i);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u < m.n) acc[0] += r.a[u] * r.a[u];
     }
-    publish<1>(g, SLOT_A, acc);
+    publish_t<1>(g, SLOT_A, acc);
     if (!grid_sync(g, 30)) { out.exit_kind = EXIT_ABORT; return false; }
     double tot[1];
     totals<1>(g, SLOT_A, tot);
@@ -256,24 +418,24 @@ __device__ bool prologue(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         out.iterations = 0;
         return false;
     }
-    double a2[2] = {0.0, 0.0};
+    T a2[2] = {T(0), T(0)};
     for (int s = g.wg; s < m.nslices; s += g.nw) {
         const int i = s * kWarp + g.lane;
         T ri = i < m.n ? v.r[i] : T(0);
         if (!cfg.x_is_zero) ri = sell_resid_row(m, s, g.lane, ri, v.x);
         if (i < m.n) {
             v.r[i] = ri;
-            a2[0] += double(ri) * double(ri);
+            a2[0] += ri * ri;
             if (store_z) {
                 if (cfg.prec == 1) {
-                    const T zi = ri / v.D[i];
+                    const T zi = jacobi(ri, v.D[i]);
                     v.z[i] = zi;
-                    a2[1] += double(ri) * double(zi);
+                    a2[1] += ri * zi;
                 }
             }
         }
     }
-    publish<2>(g, SLOT_B, a2);
+    publish_t<2>(g, SLOT_B, a2);
     if (!grid_sync(g, 31)) { out.exit_kind = EXIT_ABORT; return false; }
     double t2[2];
     totals<2>(g, SLOT_B, t2);
@@ -301,17 +463,13 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
     int iter = 1;
     for (; iter <= cfg.maxiter; ++iter) {
         if (prec == 2) {
-            double a[1] = {0.0};
+            T a[1] = {T(0)};
             const T* rr = v.r;
-            if (!ic_apply(g, m, v.D, v.r, v.w, v.z, [&](int row, T zi) {
-                    a[0] += double(rr[row]) * double(zi);
-                })) {
-                grid_sync(g, 40);
-                out.exit_kind = EXIT_ABORT;
-                return;
-            }
-            publish<1>(g, SLOT_A, a);
-            if (!grid_sync(g, 41)) { out.exit_kind = EXIT_ABORT; return; }
+            const bool ok = ic_apply(g, m, v.D, v.r, v.w, v.z, [&](int row, T zi) {
+                a[0] += rr[row] * zi;
+            });
+            publish_t<1>(g, SLOT_A, a);
+            if (!grid_sync(g, 41) || !ok) { out.exit_kind = EXIT_ABORT; return; }
             double t[1];
             totals<1>(g, SLOT_A, t);
             rho = t[0];
@@ -320,44 +478,58 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         }
         // p = z + beta p  (CG.f90:178-187)
         if (iter == 1) {
-            TF_FOR_ROWS(g, m, i) { v.p[i] = z[i]; }
+            TF_FOR4(g, m, i) { st4(v.p + i, ld4(z + i)); }
         } else {
             const T beta = T(rho / rhoold);
-            TF_FOR_ROWS(g, m, i) { v.p[i] = z[i] + beta * v.p[i]; }
+            TF_FOR4(g, m, i) {
+                const V4<T> zz = ld4(z + i);
+                V4<T> pp = ld4(v.p + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) pp.a[u] = zz.a[u] + beta * pp.a[u];
+                st4(v.p + i, pp);
+            }
         }
         if (!grid_sync(g, 42)) { out.exit_kind = EXIT_ABORT; return; }
         // q = A p; (p, q)  (CG.f90:193-218)
-        double a1[1] = {0.0};
+        T a1[1] = {T(0)};
         for (int s = g.wg; s < m.nslices; s += g.nw) {
             const int i = s * kWarp + g.lane;
             const T qi = sell_row(m, s, g.lane, v.p);
             if (i < m.n) {
                 v.q[i] = qi;
-                a1[0] += double(v.p[i]) * double(qi);
+                a1[0] += v.p[i] * qi;
             }
         }
-        publish<1>(g, SLOT_C, a1);
+        publish_t<1>(g, SLOT_C, a1);
         if (!grid_sync(g, 43)) { out.exit_kind = EXIT_ABORT; return; }
         double t1[1];
         totals<1>(g, SLOT_C, t1);
         const double alfa_d = rho / t1[0];
         const T alfa = T(alfa_d);
         // x += alfa p; r -= alfa q; ||r||; next z and rho  (CG.f90:226-253)
-        double a3[3] = {0.0, 0.0, 0.0};
-        TF_FOR_ROWS(g, m, i) {
-            const T xi = v.x[i] + alfa * v.p[i];
-            const T ri = v.r[i] - alfa * v.q[i];
-            v.x[i] = xi;
-            v.r[i] = ri;
-            a3[0] += double(ri) * double(ri);
-            if (prec == 1) {
-                const T zi = ri / v.D[i];
-                v.z[i] = zi;
-                a3[1] += double(ri) * double(zi);
+        T a3[3] = {T(0), T(0), T(0)};
+        TF_FOR4(g, m, i) {
+            V4<T> xx = ld4(v.x + i), rr = ld4(v.r + i);
+            const V4<T> pp = ld4(v.p + i), qq = ld4(v.q + i);
+            V4<T> dd, zz;
+            if (prec == 1) dd = ld4(v.D + i);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                xx.a[u] = xx.a[u] + alfa * pp.a[u];
+                rr.a[u] = rr.a[u] - alfa * qq.a[u];
+                if (prec == 1) zz.a[u] = jacobi(rr.a[u], dd.a[u]);
+                if (i + u < m.n) {
+                    a3[0] += rr.a[u] * rr.a[u];
+                    if (prec == 1) a3[1] += rr.a[u] * zz.a[u];
+                    if (nonfinite)
+                        a3[2] += (xx.a[u] == xx.a[u] ? T(1) : T(0)) + (rr.a[u] == rr.a[u] ? T(1) : T(0));
+                }
             }
-            if (nonfinite) a3[2] += (xi == xi ? 1.0 : 0.0) + (ri == ri ? 1.0 : 0.0);
+            st4(v.x + i, xx);
+            st4(v.r + i, rr);
+            if (prec == 1) st4(v.z + i, zz);
         }
-        publish<3>(g, SLOT_D, a3);
+        publish_t<3>(g, SLOT_D, a3);
         if (!grid_sync(g, 44)) { out.exit_kind = EXIT_ABORT; return; }
         double t3[3];
         totals<3>(g, SLOT_D, t3);
@@ -393,13 +565,15 @@ __device__ void cgs_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& 
     if (!prologue(g, m, v, cfg, out, tol, err, dummy, false)) return;
     const int prec = (cfg.prec == 1 || cfg.prec == 2) ? cfg.prec : 0;
     // r2 = r1 (CGS.f90:84-86); rho = (r1, r2) for the first iteration.
-    double a0[1] = {0.0};
-    TF_FOR_ROWS(g, m, i) {
-        const T ri = v.r[i];
-        v.r2[i] = ri;
-        a0[0] += double(ri) * double(ri);
+    T a0[1] = {T(0)};
+    TF_FOR4(g, m, i) {
+        const V4<T> r = ld4(v.r + i);
+        st4(v.r2 + i, r);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u < m.n) a0[0] += r.a[u] * r.a[u];
     }
-    publish<1>(g, SLOT_A, a0);
+    publish_t<1>(g, SLOT_A, a0);
     if (!grid_sync(g, 50)) { out.exit_kind = EXIT_ABORT; return; }
     double t0[1];
     totals<1>(g, SLOT_A, t0);
@@ -409,88 +583,102 @@ __device__ void cgs_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& 
     for (; iter <= cfg.maxiter; ++iter) {
         // u1 = r1 + beta q1; u2 = u1 + beta (q1 + beta u2); p2 = M^-1 u2
         const T beta = T(iter == 1 ? 0.0 : rho / rhoold);
-        TF_FOR_ROWS(g, m, i) {
-            T u1, u2;
+        TF_FOR4(g, m, i) {
+            const V4<T> rr = ld4(v.r + i);
+            V4<T> u1, u2, p2;
             if (iter == 1) {
-                u1 = v.r[i];
-                u2 = u1;
+                u1 = rr;
+                u2 = rr;
             } else {
-                const T q1 = v.q[i];
-                u1 = v.r[i] + beta * q1;
-                u2 = u1 + beta * (q1 + beta * v.u2[i]);
+                const V4<T> q1 = ld4(v.q + i);
+                u2 = ld4(v.u2 + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    u1.a[u] = rr.a[u] + beta * q1.a[u];
+                    u2.a[u] = u1.a[u] + beta * (q1.a[u] + beta * u2.a[u]);
+                }
             }
-            v.u1[i] = u1;
-            v.u2[i] = u2;
-            if (prec == 1) v.p2[i] = u2 / v.D[i];
-            else if (prec != 2) v.p2[i] = u2;
+            st4(v.u1 + i, u1);
+            st4(v.u2 + i, u2);
+            if (prec == 1) {
+                const V4<T> dd = ld4(v.D + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) p2.a[u] = jacobi(u2.a[u], dd.a[u]);
+                st4(v.p2 + i, p2);
+            } else if (prec != 2) {
+                st4(v.p2 + i, u2);
+            }
         }
         if (!grid_sync(g, 51)) { out.exit_kind = EXIT_ABORT; return; }
         if (prec == 2) {
-            if (!ic_apply(g, m, v.D, v.u2, v.w, v.p2, [](int, T) {})) {
-                grid_sync(g, 52);
-                out.exit_kind = EXIT_ABORT;
-                return;
-            }
-            if (!grid_sync(g, 53)) { out.exit_kind = EXIT_ABORT; return; }
+            const bool ok = ic_apply(g, m, v.D, v.u2, v.w, v.p2, [](int, T) {});
+            if (!grid_sync(g, 53) || !ok) { out.exit_kind = EXIT_ABORT; return; }
         }
         // v2 = A p2; alfa = rho / (r2, v2)
-        double a1[1] = {0.0};
+        T a1[1] = {T(0)};
         for (int s = g.wg; s < m.nslices; s += g.nw) {
             const int i = s * kWarp + g.lane;
             const T vi = sell_row(m, s, g.lane, v.p2);
             if (i < m.n) {
                 v.v2[i] = vi;
-                a1[0] += double(v.r2[i]) * double(vi);
+                a1[0] += v.r2[i] * vi;
             }
         }
-        publish<1>(g, SLOT_B, a1);
+        publish_t<1>(g, SLOT_B, a1);
         if (!grid_sync(g, 54)) { out.exit_kind = EXIT_ABORT; return; }
         double t1[1];
         totals<1>(g, SLOT_B, t1);
         const T alfa = T(rho / t1[0]);
         // q1 = u1 - alfa v2; p1 = M^-1 (u1 + q1); x += alfa p1
-        TF_FOR_ROWS(g, m, i) {
-            const T u1 = v.u1[i];
-            const T q1 = u1 - alfa * v.v2[i];
-            v.q[i] = q1;
-            const T tt = u1 + q1;
+        TF_FOR4(g, m, i) {
+            const V4<T> u1 = ld4(v.u1 + i), v2 = ld4(v.v2 + i);
+            V4<T> q1, tt;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                q1.a[u] = u1.a[u] - alfa * v2.a[u];
+                tt.a[u] = u1.a[u] + q1.a[u];
+            }
+            st4(v.q + i, q1);
             if (prec == 2) {
-                v.t[i] = tt;
+                st4(v.t + i, tt);
             } else {
-                const T p1 = prec == 1 ? tt / v.D[i] : tt;
-                v.p[i] = p1;
-                v.x[i] = v.x[i] + alfa * p1;
+                V4<T> p1 = tt, xx = ld4(v.x + i);
+                if (prec == 1) {
+                    const V4<T> dd = ld4(v.D + i);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) p1.a[u] = jacobi(tt.a[u], dd.a[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) xx.a[u] = xx.a[u] + alfa * p1.a[u];
+                st4(v.p + i, p1);
+                st4(v.x + i, xx);
             }
         }
         if (!grid_sync(g, 55)) { out.exit_kind = EXIT_ABORT; return; }
         if (prec == 2) {
             T* xx = v.x;
-            if (!ic_apply(g, m, v.D, v.t, v.w, v.p, [&](int row, T p1) {
-                    xx[row] = xx[row] + alfa * p1;
-                })) {
-                grid_sync(g, 56);
-                out.exit_kind = EXIT_ABORT;
-                return;
-            }
-            if (!grid_sync(g, 57)) { out.exit_kind = EXIT_ABORT; return; }
+            const bool ok = ic_apply(g, m, v.D, v.t, v.w, v.p, [&](int row, T p1) {
+                xx[row] = xx[row] + alfa * p1;
+            });
+            if (!grid_sync(g, 57) || !ok) { out.exit_kind = EXIT_ABORT; return; }
         }
         // q2 = A p1; r1 -= alfa q2; ||r1||; next rho = (r1, r2)
-        double a3[3] = {0.0, 0.0, 0.0};
+        T a3[3] = {T(0), T(0), T(0)};
         for (int s = g.wg; s < m.nslices; s += g.nw) {
             const int i = s * kWarp + g.lane;
             const T q2 = sell_row(m, s, g.lane, v.p);
             if (i < m.n) {
                 const T ri = v.r[i] - alfa * q2;
                 v.r[i] = ri;
-                a3[0] += double(ri) * double(ri);
-                a3[1] += double(ri) * double(v.r2[i]);
+                a3[0] += ri * ri;
+                a3[1] += ri * v.r2[i];
                 if (nonfinite) {
                     const T xi = v.x[i];
-                    a3[2] += (xi == xi ? 1.0 : 0.0) + (ri == ri ? 1.0 : 0.0);
+                    a3[2] += (xi == xi ? T(1) : T(0)) + (ri == ri ? T(1) : T(0));
                 }
             }
         }
-        publish<3>(g, SLOT_C, a3);
+        publish_t<3>(g, SLOT_C, a3);
         if (!grid_sync(g, 58)) { out.exit_kind = EXIT_ABORT; return; }
         double t3[3];
         totals<3>(g, SLOT_C, t3);
@@ -514,6 +702,395 @@ __device__ void cgs_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& 
     }
     out.exit_kind = EXIT_MAXITER;
     out.iterations = iter;
+}
+
+// ---- mixed precision: FP32 inner Krylov inside FP64 iterative refinement ---------
+// Outer loop in FP64: r = b - A x with the FP64 values (exact row order),
+// ||r|| and the convergence test; inner solve of A d = r in FP32 (FP32 SELL
+// values and vectors, FP64 reductions) by the same CG / CGS code with a
+// relative tolerance; x += d in FP64.  The preconditioner setup (Prec1) runs
+// once in FP64 and is rounded to FP32.
+struct MixedCfg {
+    int method;
+    int prec;
+    int max_ref;
+    int maxiter;         // cap on the total number of FP32 iterations
+    int restart;         // 1: restarted refinement; 0: reliable updates (CG)
+    int inner_maxiter;
+    double tol;
+    double inner_rtol;
+    int tol_is_relative;
+    int x_is_zero;
+};
+
+struct MixedOut {
+    int exit_kind;
+    int iterations;   // total inner iterations
+    int refinements;
+    double ini_res;
+    double fin_res;
+    double bnrm2;
+};
+
+// r64 = b - A x64, r32 = (float) r64, d32 = 0; returns ||r64|| (after a barrier).
+__device__ __forceinline__ bool mixed_residual(Grid& g, const Mat<double>& m64, const double* b64,
+                                               const double* x64, double* r64, float* r32,
+                                               float* d32, bool x_zero, double& err) {
+    double a[1] = {0.0};
+    for (int s = g.wg; s < m64.nslices; s += g.nw) {
+        const int i = s * kWarp + g.lane;
+        double ri = i < m64.n ? b64[i] : 0.0;
+        if (!x_zero) ri = sell_resid_row(m64, s, g.lane, ri, x64);
+        if (i < m64.n) {
+            r64[i] = ri;
+            r32[i] = (float)ri;
+            if (d32) d32[i] = 0.0f;
+            a[0] += ri * ri;
+        }
+    }
+    publish<1>(g, SLOT_D + 3, a);
+    if (!grid_sync(g, 70)) return false;
+    double t[1];
+    totals<1>(g, SLOT_D + 3, t);
+    err = sqrt(t[0]);
+    return true;
+}
+
+__device__ void mixed_solve(Grid& g, const Mat<double>& m64, const Mat<float>& m32, double* x64,
+                            double* r64, const double* b64, double* D64, Vecs<float>& v32,
+                            const MixedCfg& c, MixedOut& out) {
+    out.exit_kind = EXIT_ABORT;
+    if (!prec1_phase(g, m64, D64, c.prec)) return;
+    // D64 was written in slice order; the next pass reads it four rows per
+    // thread, so it must be complete first.
+    if (!grid_sync(g, 74)) return;
+    double acc[1] = {0.0};
+    TF_FOR4(g, m64, i) {
+        const V4<double> d = ld4(D64 + i), bb = ld4(b64 + i);
+        V4<float> df, wf;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            // FP32 solves hold 1/D for the diagonal preconditioner
+            df.a[u] = c.prec == 1 ? (float)(1.0 / d.a[u]) : (float)d.a[u];
+            wf.a[u] = Cell<float>::sentinel();
+            if (i + u < m64.n) acc[0] += bb.a[u] * bb.a[u];
+        }
+        st4(v32.D + i, df);
+        st4(v32.w + i, wf);
+    }
+    publish<1>(g, SLOT_A, acc);
+    if (!grid_sync(g, 71)) return;
+    double tot[1];
+    totals<1>(g, SLOT_A, tot);
+    const double bnrm2 = sqrt(tot[0]);
+    out.bnrm2 = bnrm2;
+    double tol = c.tol_is_relative ? c.tol * bnrm2 : c.tol;
+    if (bnrm2 < tol || (c.tol_is_relative && bnrm2 == 0.0)) {
+        out.exit_kind = EXIT_BNRM;
+        out.iterations = 0;
+        return;
+    }
+    double err;
+    if (!mixed_residual(g, m64, b64, x64, r64, v32.r, v32.x, c.x_is_zero != 0, err)) return;
+    out.ini_res = err;
+    out.fin_res = err;
+    if (err < tol) {
+        out.exit_kind = EXIT_INIRES;
+        out.iterations = 0;
+        return;
+    }
+    SolveCfg ci;
+    ci.method = c.method;
+    ci.prec = c.prec;
+    ci.maxiter = c.inner_maxiter;
+    ci.tol = c.inner_rtol;
+    ci.x_is_zero = 1;
+    ci.do_prec1 = 0;
+    ci.tol_is_relative = 1;
+    int total = 0, stall = 0;
+    double prev = err;
+    for (int ref = 1; ref <= c.max_ref; ++ref) {
+        ci.maxiter = min(c.inner_maxiter, c.maxiter - total);
+        if (ci.maxiter <= 0) break;
+        SolveOut oi;
+        oi.exit_kind = 0;
+        oi.iterations = 0;
+        oi.fin_res = 0.0;
+        if (c.method == 2) cgs_solve<float>(g, m32, v32, ci, oi);
+        else cg_solve<float>(g, m32, v32, ci, oi);
+        if (oi.exit_kind == EXIT_ABORT) return;
+        total += oi.exit_kind == EXIT_MAXITER || oi.exit_kind == EXIT_NONFINITE ? ci.maxiter
+                                                                                 : oi.iterations;
+        out.iterations = total;
+        out.refinements = ref;
+        if (!isfinite(oi.fin_res)) {
+            out.exit_kind = EXIT_NONFINITE;
+            return;
+        }
+        TF_FOR4(g, m64, i) {
+            V4<double> xx = ld4(x64 + i);
+            const V4<float> d = ld4(v32.x + i);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xx.a[u] = xx.a[u] + (double)d.a[u];
+            st4(x64 + i, xx);
+        }
+        if (!grid_sync(g, 72)) return;
+        // r = b - A x; d32 is kept (not cleared) until the step is accepted
+        double err_new;
+        if (!mixed_residual(g, m64, b64, x64, r64, v32.r, nullptr, false, err_new)) return;
+        if (!(err_new <= 10.0 * prev)) {
+            // The correction made the true residual grow tenfold (the inner
+            // iteration diverged in FP32): take the step back and stop.  (CG
+            // minimises the error in the A-norm, so a smaller rise of the
+            // residual norm is normal and is kept.)
+            TF_FOR4(g, m64, i) {
+                V4<double> xx = ld4(x64 + i);
+                const V4<float> d = ld4(v32.x + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) xx.a[u] = xx.a[u] - (double)d.a[u];
+                st4(x64 + i, xx);
+            }
+            if (!grid_sync(g, 73)) return;
+            if (!mixed_residual(g, m64, b64, x64, r64, v32.r, v32.x, false, err)) return;
+            out.fin_res = err;
+            out.exit_kind = isfinite(err_new) ? EXIT_MAXITER : EXIT_NONFINITE;
+            return;
+        }
+        err = err_new;
+        TF_FOR4(g, m64, i) { st4(v32.x + i, V4<float>{{0.f, 0.f, 0.f, 0.f}}); }
+        out.fin_res = err;
+        if (err < tol) {
+            out.exit_kind = EXIT_CONVERGED;
+            return;
+        }
+        stall = err > 0.9 * prev ? stall + 1 : 0;
+        if (stall >= 6) break;
+        prev = err;
+    }
+    out.exit_kind = EXIT_MAXITER;
+}
+
+// ---- mixed precision CG with reliable updates ---------------------------------
+// One FP32 preconditioned CG iteration stream (FP32 values and vectors, FP64
+// reductions).  Whenever its recursive residual has dropped by `inner_rtol`
+// since the last refinement (or below the tolerance), the FP32 correction is
+// added to x in FP64, the true residual b - A x is recomputed with the FP64
+// values, the convergence test ||r|| < tol is made on it in FP64, and the
+// FP32 residual is replaced by it.  Unlike a restarted refinement the search
+// direction is kept, so the iteration count stays close to the FP64 solve's.
+__device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const Mat<float>& m32,
+                                  double* x64, double* r64, const double* b64, double* D64,
+                                  double* xbest, Vecs<float>& v, const MixedCfg& c,
+                                  MixedOut& out) {
+    out.exit_kind = EXIT_ABORT;
+    const int prec = (c.prec == 1 || c.prec == 2) ? c.prec : 0;
+    if (!prec1_phase(g, m64, D64, c.prec)) return;
+    if (!grid_sync(g, 80)) return;
+    double acc[1] = {0.0};
+    TF_FOR4(g, m64, i) {
+        const V4<double> d = ld4(D64 + i), bb = ld4(b64 + i);
+        V4<float> df, wf;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            // FP32 solves hold 1/D for the diagonal preconditioner
+            df.a[u] = c.prec == 1 ? (float)(1.0 / d.a[u]) : (float)d.a[u];
+            wf.a[u] = Cell<float>::sentinel();
+            if (i + u < m64.n) acc[0] += bb.a[u] * bb.a[u];
+        }
+        st4(v.D + i, df);
+        st4(v.w + i, wf);
+    }
+    publish<1>(g, SLOT_A, acc);
+    if (!grid_sync(g, 81)) return;
+    double tot[1];
+    totals<1>(g, SLOT_A, tot);
+    const double bnrm2 = sqrt(tot[0]);
+    out.bnrm2 = bnrm2;
+    const double tol = c.tol_is_relative ? c.tol * bnrm2 : c.tol;
+    if (bnrm2 < tol || (c.tol_is_relative && bnrm2 == 0.0)) {
+        out.exit_kind = EXIT_BNRM;
+        out.iterations = 0;
+        return;
+    }
+    const float* z = prec == 0 ? v.r : v.z;
+    // r64 = b - A x; r = (float) r64; xl = 0; ||r||; z = M^-1 r (diag) and (r, z)
+    auto refresh = [&](bool x_zero, double& err, double& rz) -> bool {
+        double a[2] = {0.0, 0.0};
+        for (int s = g.wg; s < m64.nslices; s += g.nw) {
+            const int i = s * kWarp + g.lane;
+            double ri = i < m64.n ? b64[i] : 0.0;
+            if (!x_zero) ri = sell_resid_row(m64, s, g.lane, ri, x64);
+            if (i < m64.n) {
+                r64[i] = ri;
+                const float rf = (float)ri;
+                v.r[i] = rf;
+                v.x[i] = 0.0f;
+                a[0] += ri * ri;
+                if (prec == 1) {
+                    const float zf = rf * v.D[i];
+                    v.z[i] = zf;
+                    a[1] += double(rf * zf);
+                } else if (prec == 0) {
+                    a[1] += double(rf * rf);
+                }
+            }
+        }
+        publish<2>(g, SLOT_D, a);
+        if (!grid_sync(g, 82)) return false;
+        double t[2];
+        totals<2>(g, SLOT_D, t);
+        err = sqrt(t[0]);
+        rz = t[1];
+        return true;
+    };
+    auto ic = [&](double& rz) -> bool {
+        float a[1] = {0.f};
+        const float* rr = v.r;
+        const bool ok = ic_apply(g, m32, v.D, v.r, v.w, v.z, [&](int row, float zi) {
+            a[0] += rr[row] * zi;
+        });
+        publish_t<1>(g, SLOT_A, a);
+        if (!grid_sync(g, 83) || !ok) return false;
+        double t[1];
+        totals<1>(g, SLOT_A, t);
+        rz = t[0];
+        return true;
+    };
+    double err, rz;
+    if (!refresh(c.x_is_zero != 0, err, rz)) return;
+    out.ini_res = err;
+    out.fin_res = err;
+    if (err < tol) {
+        out.exit_kind = EXIT_INIRES;
+        out.iterations = 0;
+        return;
+    }
+    if (prec == 2 && !ic(rz)) return;
+    // best FP64 iterate so far (returned if the iteration later diverges)
+    auto keep_best = [&]() {
+        TF_FOR4(g, m64, i) { st4(xbest + i, ld4(x64 + i)); }
+    };
+    keep_best();
+    double rho = rz, maxr = err, prev = err, best = err;
+    int nref = 0, stall = 0, it = 1;
+    bool diverged = false;
+    const double delta = c.inner_rtol > 0.0 && c.inner_rtol < 1.0 ? c.inner_rtol : 0.1;
+    float beta = 0.0f;
+    for (; it <= c.maxiter; ++it) {
+        if (it == 1) {
+            TF_FOR4(g, m32, i) { st4(v.p + i, ld4(z + i)); }
+        } else {
+            TF_FOR4(g, m32, i) {
+                const V4<float> zz = ld4(z + i);
+                V4<float> pp = ld4(v.p + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) pp.a[u] = zz.a[u] + beta * pp.a[u];
+                st4(v.p + i, pp);
+            }
+        }
+        if (!grid_sync(g, 84)) return;
+        float a1[1] = {0.f};
+        for (int s = g.wg; s < m32.nslices; s += g.nw) {
+            const int i = s * kWarp + g.lane;
+            const float qi = sell_row(m32, s, g.lane, v.p);
+            if (i < m32.n) {
+                v.q[i] = qi;
+                a1[0] += v.p[i] * qi;
+            }
+        }
+        publish_t<1>(g, SLOT_C, a1);
+        if (!grid_sync(g, 85)) return;
+        double t1[1];
+        totals<1>(g, SLOT_C, t1);
+        const float alfa = (float)(rho / t1[0]);
+        float a3[2] = {0.f, 0.f};
+        TF_FOR4(g, m32, i) {
+            V4<float> xx = ld4(v.x + i), rr = ld4(v.r + i), zz;
+            const V4<float> pp = ld4(v.p + i), qq = ld4(v.q + i);
+            V4<float> dd;
+            if (prec == 1) dd = ld4(v.D + i);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                xx.a[u] = xx.a[u] + alfa * pp.a[u];
+                rr.a[u] = rr.a[u] - alfa * qq.a[u];
+                if (prec == 1) zz.a[u] = jacobi(rr.a[u], dd.a[u]);
+                if (i + u < m32.n) {
+                    a3[0] += rr.a[u] * rr.a[u];
+                    if (prec == 1) a3[1] += rr.a[u] * zz.a[u];
+                }
+            }
+            st4(v.x + i, xx);
+            st4(v.r + i, rr);
+            if (prec == 1) st4(v.z + i, zz);
+        }
+        publish_t<2>(g, SLOT_B, a3);
+        if (!grid_sync(g, 86)) return;
+        double t3[2];
+        totals<2>(g, SLOT_B, t3);
+        const double rnorm = sqrt(t3[0]);
+        out.iterations = it;
+        rz = prec == 1 ? t3[1] : t3[0];
+        if (!isfinite(rnorm)) {
+            out.exit_kind = EXIT_NONFINITE;
+            return;
+        }
+        if (rnorm < delta * maxr || rnorm < tol) {
+            // refinement: x += xl in FP64, true residual, FP64 test
+            TF_FOR4(g, m64, i) {
+                V4<double> xd = ld4(x64 + i);
+                const V4<float> xl = ld4(v.x + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) xd.a[u] = xd.a[u] + (double)xl.a[u];
+                st4(x64 + i, xd);
+            }
+            if (!grid_sync(g, 87)) return;
+            if (!refresh(false, err, rz)) return;
+            out.fin_res = err;
+            out.refinements = ++nref;
+            if (err < tol) {
+                out.exit_kind = EXIT_CONVERGED;
+                return;
+            }
+            if (!isfinite(err)) {
+                out.exit_kind = EXIT_NONFINITE;
+                return;
+            }
+            if (err < best) {
+                best = err;
+                keep_best();
+            } else if (err > 1e3 * best) {
+                diverged = true;
+                break;
+            }
+            stall = err > 0.999 * prev ? stall + 1 : 0;
+            if (stall >= 4) break;
+            prev = err;
+            maxr = err;
+        }
+        if (prec == 2 && !ic(rz)) return;
+        beta = (float)(rz / rho);
+        rho = rz;
+    }
+    // out of iterations: fold the pending correction into x, and fall back
+    // to the best iterate if this one is worse
+    if (!diverged) {
+        TF_FOR4(g, m64, i) {
+            V4<double> xd = ld4(x64 + i);
+            const V4<float> xl = ld4(v.x + i);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xd.a[u] = xd.a[u] + (double)xl.a[u];
+            st4(x64 + i, xd);
+        }
+        if (!grid_sync(g, 88)) return;
+        if (!refresh(false, err, rz)) return;
+    }
+    if (diverged || !(err <= best)) {
+        TF_FOR4(g, m64, i) { st4(x64 + i, ld4(xbest + i)); }
+        if (!grid_sync(g, 89)) return;
+        if (!refresh(false, err, rz)) return;
+    }
+    out.fin_res = err;
+    out.exit_kind = err < tol ? EXIT_CONVERGED : EXIT_MAXITER;
 }
 
 }  // namespace tflows

@@ -64,7 +64,8 @@ void default_opts(tflows_options* o) {
     std::memset(o, 0, sizeof(*o));
     o->precision = TFLOWS_FP64;
     o->tol_mode = TFLOWS_TOL_ABSOLUTE;
-    o->inner_rtol = 1e-4;
+    o->inner_rtol = 1e-1;
+    o->refine_restart = 1;
     o->inner_maxiter = 2000;
     o->max_refinements = 30;
     o->ic_sweeps = 0;
@@ -128,9 +129,13 @@ cudaError_t upload(T** dst, const T* src, size_t count) {
 
 void free_topology_arrays(DeviceTopology& t) {
     for (void* p : {(void*)t.rowptr, (void*)t.col, (void*)t.soff, (void*)t.scol, (void*)t.meta,
-                    (void*)t.perm_f, (void*)t.perm_b, (void*)t.tpos})
+                    (void*)t.perm_f, (void*)t.perm_b, (void*)t.tpos, (void*)t.chunk_lev_f,
+                    (void*)t.chunk_lev_b, (void*)t.lev_nch_f, (void*)t.lev_nch_b,
+                    (void*)t.lev_cnt})
         if (p) cudaFree(p);
     t.rowptr = t.col = t.scol = t.meta = t.perm_f = t.perm_b = t.tpos = nullptr;
+    t.chunk_lev_f = t.chunk_lev_b = t.lev_nch_f = t.lev_nch_b = nullptr;
+    t.lev_cnt = nullptr;
     t.soff = nullptr;
 }
 
@@ -170,7 +175,8 @@ cudaError_t build_levels(DeviceTopology& t) {
     if (t.levels_built) return cudaSuccess;
     const int n = t.n;
     std::vector<int> lev((size_t)n);
-    auto make_perm = [&](bool forward, int** out, int* nchunk, int* nlev) -> cudaError_t {
+    auto make_perm = [&](bool forward, int** out, int* nchunk, int* nlev, int** chunk_lev,
+                         int** lev_nch) -> cudaError_t {
         int maxl = -1;
         if (forward) {
             for (int i = 0; i < n; ++i) {
@@ -198,11 +204,21 @@ cudaError_t build_levels(DeviceTopology& t) {
         for (int i = 0; i < n; ++i) perm[fill[lev[i]]++] = i;
         *nchunk = (int)(start[L] / 32);
         *nlev = L;
-        return upload(out, perm.data(), perm.size());
+        std::vector<int> clev((size_t)std::max(*nchunk, 1), 0), nch((size_t)L, 0);
+        for (int l = 0; l < L; ++l) {
+            nch[l] = (int)((start[l + 1] - start[l]) / 32);
+            for (long long c = start[l] / 32; c < start[l + 1] / 32; ++c) clev[c] = l;
+        }
+        cudaError_t e = upload(out, perm.data(), perm.size());
+        if (e == cudaSuccess) e = upload(chunk_lev, clev.data(), clev.size());
+        if (e == cudaSuccess) e = upload(lev_nch, nch.data(), nch.size());
+        return e;
     };
-    cudaError_t e = make_perm(true, &t.perm_f, &t.nchunk_f, &t.nlev_f);
+    cudaError_t e = make_perm(true, &t.perm_f, &t.nchunk_f, &t.nlev_f, &t.chunk_lev_f, &t.lev_nch_f);
     if (e != cudaSuccess) return e;
-    e = make_perm(false, &t.perm_b, &t.nchunk_b, &t.nlev_b);
+    e = make_perm(false, &t.perm_b, &t.nchunk_b, &t.nlev_b, &t.chunk_lev_b, &t.lev_nch_b);
+    if (e != cudaSuccess) return e;
+    e = cudaMalloc(&t.lev_cnt, sizeof(unsigned) * (size_t)(t.nlev_f + t.nlev_b));
     if (e != cudaSuccess) return e;
     t.levels_built = true;
     return cudaSuccess;
@@ -347,6 +363,7 @@ SolveRequest make_request(const tflows_options& o, int method, int prec, int max
     rq.inner_maxiter = o.inner_maxiter;
     rq.max_refinements = o.max_refinements;
     rq.ic_sweeps = o.ic_sweeps;
+    rq.refine_restart = o.refine_restart;
     rq.timeout_s = o.timeout_s > 0 ? o.timeout_s : 5.0;
     rq.block = o.block_size;
     rq.grid = o.grid_blocks;
@@ -373,7 +390,6 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
              double* d_x, double* d_r_out, cudaStream_t s, SolveReport& rep) {
     SolveRequest rq = rq0;
     if (rq.method == TFLOWS_METHOD_BICG_TRUE) return fail(TFLOWS_UNSUPPORTED, "true BiCG not built");
-    if (rq.precision != TFLOWS_FP64) return fail(TFLOWS_UNSUPPORTED, "mixed precision not built");
     if (rq.prec == 2) {
         if (!tp->t.ic_ok)
             return fail(TFLOWS_BAD_INPUT,
@@ -386,17 +402,22 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
     if (e != cudaSuccess) return cuda_fail(e, "workspace");
     if ((e = permute_values(tp->t, tp->ws, d_val, true, rq.precision != TFLOWS_FP64, s)) != cudaSuccess)
         return cuda_fail(e, "value layout");
+    // The kernels work on padded, 16-byte aligned workspace vectors: x and b
+    // are staged into workspace slots 11 and 12 unless they already are them.
+    const size_t nb = sizeof(double) * tp->t.n;
+    double* X = ws_vec(tp, 11);
     double* R = ws_vec(tp, 12);
-    if ((e = cudaMemcpyAsync(R, d_b, sizeof(double) * tp->t.n, cudaMemcpyDeviceToDevice, s)) !=
-        cudaSuccess)
+    if (d_x != X && (e = cudaMemcpyAsync(X, d_x, nb, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "copy x");
+    if ((e = cudaMemcpyAsync(R, d_b, nb, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
         return cuda_fail(e, "copy b");
-    int st = run_solve(tp->t, tp->ws, rq, d_x, R, s, rep);
+    int st = run_solve(tp->t, tp->ws, rq, X, R, s, rep);
     if (st == TFLOWS_CUDA_ERROR) return fail(st, rep.message);
-    if (d_r_out) {
-        e = cudaMemcpyAsync(d_r_out, R, sizeof(double) * tp->t.n, cudaMemcpyDeviceToDevice, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return cuda_fail(e, "copy r");
-    }
+    if (d_x != X && (e = cudaMemcpyAsync(d_x, X, nb, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "copy x back");
+    if (d_r_out && (e = cudaMemcpyAsync(d_r_out, R, nb, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "copy r");
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "sync");
     t_status = st;
     t_error = rep.message;
     return st;
