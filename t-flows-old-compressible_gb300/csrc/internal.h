@@ -22,6 +22,7 @@ struct DeviceTopology {
     bool levels_built = false;
     int nlev_f = 0, nlev_b = 0;
     int nchunk_f = 0, nchunk_b = 0;
+    int wide_f = 0, wide_b = 0;  // chunks in the widest level
     // device arrays
     int* rowptr = nullptr;     // 0-based, n + 1
     int* col = nullptr;        // 0-based, nnz

@@ -226,6 +226,8 @@ Mat<T> make_mat(const DeviceTopology& t, const T* sval) {
     m.cnt_b = t.lev_cnt ? t.lev_cnt + t.nlev_f : nullptr;
     m.nchunk_f = t.nchunk_f;
     m.nchunk_b = t.nchunk_b;
+    m.wide_f = t.wide_f;
+    m.wide_b = t.wide_b;
     return m;
 }
 

@@ -52,6 +52,8 @@ struct Mat {
     unsigned* cnt_b;
     int nchunk_f;
     int nchunk_b;
+    int wide_f;  // chunks in the widest forward / backward level
+    int wide_b;
 };
 
 template <typename T>
@@ -216,83 +218,105 @@ __device__ __forceinline__ T diag_value(const Mat<T>& m, int i) {
 // which sit in chunks of lower index, so with all warps resident the sweep
 // cannot deadlock.
 constexpr int kSweepMax = 8;  // dependencies prefetched per row
-// Pause between polls of not-yet-ready cells, in ns (0: poll back to back).
+// Longest pause between polls of not-yet-ready cells, in ns (0: poll back to
+// back).
 #ifndef TFLOWS_SWEEP_SLEEP
-#define TFLOWS_SWEEP_SLEEP 0
+#define TFLOWS_SWEEP_SLEEP 512
+#endif
+// Warps taking part in a sweep: no more than the widest level has chunks,
+// so each warp's next chunk is about one level ahead of the current one.
+#ifndef TFLOWS_SWEEP_WARPS_PER_CHUNK
+#define TFLOWS_SWEEP_WARPS_PER_CHUNK 4
 #endif
 
-// Wait for up to kSweepMax cells at once: all not-yet-ready cells are
-// re-polled together after each short sleep, so a row pays one round trip
-// after its last dependency lands instead of one per dependency.
-template <typename T>
-__device__ __forceinline__ bool wait_cells(const T* cells, const int (&c)[kSweepMax], int n,
-                                           T (&v)[kSweepMax], const Grid& g, int where) {
+__device__ __forceinline__ int sweep_warps(const Grid& g, int wide) {
+    const int want = max(1, wide * TFLOWS_SWEEP_WARPS_PER_CHUNK);
+    return want < g.nw ? want : g.nw;
+}
+
+// One chunk of a level-ordered sweep.  Each lane owns one row; every index,
+// coefficient and own-row operand is loaded before the first poll.  The
+// warp then polls its rows' not-yet-ready dependency cells together, and a
+// lane computes and publishes its row as soon as its own dependencies are
+// in, without waiting for the other lanes, so a level's rows become visible
+// one handoff after their inputs rather than after the slowest lane of the
+// chunk.  Rows with more than kSweepMax dependencies wait one cell at a time.
+// KIND 0: forward  acc = rhs - sum a_t cell_t,   result = acc * D_row
+// KIND 1: backward acc = mid - sum a_t cell_t,   result = acc * D_row
+// KIND 2: pivots   acc = a_ii - sum cell_t a_t a_t, result = 1 / acc
+template <int KIND, typename T, typename Pub>
+__device__ __forceinline__ bool sweep_chunk(const Grid& g, const Mat<T>& m, int row, int t0, int t1,
+                                            long long base, T acc, T dmul, const T* cells,
+                                            int where, Pub publish_row) {
     using C = Cell<T>;
+    const int n = row >= 0 ? t1 - t0 : 0;
+    const bool longrow = n > kSweepMax;  // rare: walked with a cursor instead
+    int c[kSweepMax];
+    T a[kSweepMax], v[kSweepMax];
     unsigned pending = 0;
 #pragma unroll
     for (int u = 0; u < kSweepMax; ++u) {
-        if (u < n) {
-            const auto b = C::load(cells + c[u]);
-            if (b == C::kSentinel) pending |= 1u << u;
-            else v[u] = C::value(b);
-        }
+        const bool use = !longrow && u < n;
+        c[u] = use ? m.scol[base + 32LL * (t0 + u)] : 0;
+        a[u] = use ? m.sval[base + 32LL * (t0 + u)] : T(0);
+        v[u] = T(0);
+        if (use) pending |= 1u << u;
     }
-    if (!pending) return true;
-    const long long t0 = globaltimer_ns();
+    int cursor = t0;
+    bool done = row < 0;
+    const long long start = globaltimer_ns();
     unsigned spins = 0;
-    while (pending) {
-        if (TFLOWS_SWEEP_SLEEP > 0) __nanosleep(TFLOWS_SWEEP_SLEEP);
+    while (true) {
+        if (!done) {
+            if (longrow) {
+                while (cursor < t1) {
+                    const auto b = C::load(cells + m.scol[base + 32LL * cursor]);
+                    if (b == C::kSentinel) break;
+                    const T av = m.sval[base + 32LL * cursor];
+                    const T vv = C::value(b);
+                    acc = KIND == 2 ? acc - vv * av * av : acc - av * vv;
+                    ++cursor;
+                }
+                if (cursor == t1) {
+                    publish_row(KIND == 2 ? T(1) / acc : acc * dmul);
+                    done = true;
+                }
+            } else {
 #pragma unroll
-        for (int u = 0; u < kSweepMax; ++u) {
-            if (pending & (1u << u)) {
-                const auto b = C::load(cells + c[u]);
-                if (b != C::kSentinel) {
-                    v[u] = C::value(b);
-                    pending &= ~(1u << u);
+                for (int u = 0; u < kSweepMax; ++u) {
+                    if (pending & (1u << u)) {
+                        const auto b = C::load(cells + c[u]);
+                        if (b != C::kSentinel) {
+                            v[u] = C::value(b);
+                            pending &= ~(1u << u);
+                        }
+                    }
+                }
+                if (!pending) {
+                    // every input present: sum in slot order (the reference's order)
+#pragma unroll
+                    for (int u = 0; u < kSweepMax; ++u)
+                        if (u < n) acc = KIND == 2 ? acc - v[u] * a[u] * a[u] : acc - a[u] * v[u];
+                    publish_row(KIND == 2 ? T(1) / acc : acc * dmul);
+                    done = true;
                 }
             }
         }
-        if ((++spins & 63u) == 0u && pending) {
-            if (ld_relaxed_s32(&g.ctl->abort)) return false;
-            if (globaltimer_ns() - t0 > g.timeout_ns) {
+        if (__all_sync(0xffffffffu, done)) return true;
+        // back off while the inputs are far from ready (a chunk several
+        // levels ahead of the front), never more than TFLOWS_SWEEP_SLEEP ns
+        ++spins;
+        if (TFLOWS_SWEEP_SLEEP > 0 && spins > 4u)
+            __nanosleep(min((unsigned)TFLOWS_SWEEP_SLEEP, 8u << min(spins - 4u, 10u)));
+        if ((spins & 63u) == 0u) {
+            bool quit = ld_relaxed_s32(&g.ctl->abort) != 0;
+            if (!quit && globaltimer_ns() - start > g.timeout_ns) {
                 raise_abort(g.ctl, ST_TIMEOUT, where);
-                return false;
+                quit = true;
             }
+            if (__any_sync(0xffffffffu, quit)) return false;
         }
     }
-    return true;
-}
-
-// Forward-type row: acc - sum_{t in [t0,t1)} a_t * cell[col_t], summed in
-// slot order (the reference's order) once every cell has its value.
-template <typename T>
-__device__ __forceinline__ bool sweep_row(const Grid& g, const Mat<T>& m, long long base, int t0,
-                                          int t1, T acc, const T* cells, int where, T& out) {
-    const int n = t1 - t0;
-    if (n <= kSweepMax) {
-        int c[kSweepMax];
-        T a[kSweepMax], v[kSweepMax];
-#pragma unroll
-        for (int u = 0; u < kSweepMax; ++u) {
-            c[u] = u < n ? m.scol[base + 32LL * (t0 + u)] : 0;
-            a[u] = u < n ? m.sval[base + 32LL * (t0 + u)] : T(0);
-            v[u] = T(0);
-        }
-        if (!wait_cells(cells, c, n, v, g, where)) return false;
-#pragma unroll
-        for (int u = 0; u < kSweepMax; ++u)
-            if (u < n) acc = acc - a[u] * v[u];
-    } else {
-        for (int t = t0; t < t1; ++t) {
-            const int k = m.scol[base + 32LL * t];
-            const T av = m.sval[base + 32LL * t];
-            T v;
-            if (!wait_cell(cells + k, v, g.ctl, g.timeout_ns, where)) return false;
-            acc = acc - av * v;
-        }
-    }
-    out = acc;
-    return true;
 }
 
 // ---- Prec1 -----------------------------------------------------------------
@@ -304,37 +328,19 @@ __device__ bool prec1_phase(Grid& g, const Mat<T>& m, T* D, int prec) {
         TF_FOR_ROWS(g, m, i) { D[i] = Cell<T>::sentinel(); }
         if (!grid_sync(g, 10)) return false;
         bool ok = true;
-        for (int ch = g.wg; ch < m.nchunk_f && ok; ch += g.nw) {
+        const int nws = sweep_warps(g, m.wide_f);
+        for (int ch = g.wg; g.wg < nws && ch < m.nchunk_f && ok; ch += nws) {
             const int row = m.perm_f[ch * kWarp + g.lane];
+            int dslot = 0;
+            long long base = 0;
+            T aii = T(1);
             if (row >= 0) {
-                const int dslot = m.meta[row] >> 16;
-                const long long base = m.soff[row >> 5] + (row & 31);
-                T sum = m.sval[base + 32LL * dslot];
-                int c[kSweepMax];
-                T a[kSweepMax];
-                if (dslot <= kSweepMax) {
-                    T dv[kSweepMax];
-#pragma unroll
-                    for (int u = 0; u < kSweepMax; ++u) {
-                        c[u] = u < dslot ? m.scol[base + 32LL * u] : 0;
-                        a[u] = u < dslot ? m.sval[base + 32LL * u] : T(0);
-                        dv[u] = T(0);
-                    }
-                    ok = wait_cells(D, c, dslot, dv, g, 11);
-#pragma unroll
-                    for (int u = 0; u < kSweepMax; ++u)
-                        if (u < dslot) sum = sum - dv[u] * a[u] * a[u];
-                } else {
-                    for (int t = 0; t < dslot && ok; ++t) {
-                        const int k = m.scol[base + 32LL * t];
-                        const T av = m.sval[base + 32LL * t];
-                        T dk;
-                        ok = wait_cell(D + k, dk, g.ctl, g.timeout_ns, 11);
-                        sum = sum - dk * av * av;
-                    }
-                }
-                Cell<T>::store(D + row, T(1) / sum);
+                dslot = m.meta[row] >> 16;
+                base = m.soff[row >> 5] + (row & 31);
+                aii = m.sval[base + 32LL * dslot];
             }
+            ok = sweep_chunk<2>(g, m, row, 0, dslot, base, aii, T(1), D, 11,
+                                [&](T d) { Cell<T>::store(D + row, d); });
         }
         const bool synced = grid_sync(g, 12);
         return ok && synced;
@@ -352,35 +358,43 @@ __device__ bool prec1_phase(Grid& g, const Mat<T>& m, T* D, int prec) {
 template <typename T, typename Epi>
 __device__ bool ic_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* w, T* z, Epi epi) {
     bool ok = true;
-    for (int ch = g.wg; ch < m.nchunk_f && ok; ch += g.nw) {
+    const int nwf = sweep_warps(g, m.wide_f);
+    for (int ch = g.wg; g.wg < nwf && ch < m.nchunk_f && ok; ch += nwf) {
         const int row = m.perm_f[ch * kWarp + g.lane];
+        int dslot = 0;
+        long long base = 0;
+        T r0 = T(0), d = T(0);
         if (row >= 0) {
-            const int dslot = m.meta[row] >> 16;
-            const long long base = m.soff[row >> 5] + (row & 31);
-            const T d = D[row];
-            T sum;
-            ok = sweep_row(g, m, base, 0, dslot, rhs[row], w, 20, sum);
-            if (ok) Cell<T>::store(w + row, sum * d);
+            dslot = m.meta[row] >> 16;
+            base = m.soff[row >> 5] + (row & 31);
+            r0 = rhs[row];
+            d = D[row];
             z[row] = Cell<T>::sentinel();
         }
+        ok = sweep_chunk<0>(g, m, row, 0, dslot, base, r0, d, w, 20,
+                            [&](T val) { Cell<T>::store(w + row, val); });
     }
     if (!grid_sync(g, 21) || !ok) return false;
-    for (int ch = g.wg; ch < m.nchunk_b && ok; ch += g.nw) {
+    const int nwb = sweep_warps(g, m.wide_b);
+    for (int ch = g.wg; g.wg < nwb && ch < m.nchunk_b && ok; ch += nwb) {
         const int row = m.perm_b[ch * kWarp + g.lane];
+        int dslot = 0, len = 0;
+        long long base = 0;
+        T mid = T(0), d = T(0);
         if (row >= 0) {
             const int meta = m.meta[row];
-            const int len = meta & 0xFFFF, dslot = meta >> 16;
-            const long long base = m.soff[row >> 5] + (row & 31);
-            const T d = D[row];
-            T sum;
-            ok = sweep_row(g, m, base, dslot + 1, len, w[row] / (d + T(kTiny)), z, 22, sum);
-            if (ok) {
-                const T zi = sum * d;
-                Cell<T>::store(z + row, zi);
-                w[row] = Cell<T>::sentinel();
-                epi(row, zi);
-            }
+            len = meta & 0xFFFF;
+            dslot = meta >> 16;
+            base = m.soff[row >> 5] + (row & 31);
+            d = D[row];
+            mid = w[row] / (d + T(kTiny));
         }
+        ok = sweep_chunk<1>(g, m, row, dslot + 1, row >= 0 ? len : dslot + 1, base, mid, d, z, 22,
+                            [&](T zi) {
+                                Cell<T>::store(z + row, zi);
+                                w[row] = Cell<T>::sentinel();
+                                epi(row, zi);
+                            });
     }
     return ok;
 }

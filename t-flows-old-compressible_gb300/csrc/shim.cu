@@ -176,7 +176,7 @@ cudaError_t build_levels(DeviceTopology& t) {
     const int n = t.n;
     std::vector<int> lev((size_t)n);
     auto make_perm = [&](bool forward, int** out, int* nchunk, int* nlev, int** chunk_lev,
-                         int** lev_nch) -> cudaError_t {
+                         int** lev_nch, int* wide) -> cudaError_t {
         int maxl = -1;
         if (forward) {
             for (int i = 0; i < n; ++i) {
@@ -205,8 +205,10 @@ cudaError_t build_levels(DeviceTopology& t) {
         *nchunk = (int)(start[L] / 32);
         *nlev = L;
         std::vector<int> clev((size_t)std::max(*nchunk, 1), 0), nch((size_t)L, 0);
+        *wide = 0;
         for (int l = 0; l < L; ++l) {
             nch[l] = (int)((start[l + 1] - start[l]) / 32);
+            *wide = std::max(*wide, nch[l]);
             for (long long c = start[l] / 32; c < start[l + 1] / 32; ++c) clev[c] = l;
         }
         cudaError_t e = upload(out, perm.data(), perm.size());
@@ -214,9 +216,11 @@ cudaError_t build_levels(DeviceTopology& t) {
         if (e == cudaSuccess) e = upload(lev_nch, nch.data(), nch.size());
         return e;
     };
-    cudaError_t e = make_perm(true, &t.perm_f, &t.nchunk_f, &t.nlev_f, &t.chunk_lev_f, &t.lev_nch_f);
+    cudaError_t e = make_perm(true, &t.perm_f, &t.nchunk_f, &t.nlev_f, &t.chunk_lev_f, &t.lev_nch_f,
+                              &t.wide_f);
     if (e != cudaSuccess) return e;
-    e = make_perm(false, &t.perm_b, &t.nchunk_b, &t.nlev_b, &t.chunk_lev_b, &t.lev_nch_b);
+    e = make_perm(false, &t.perm_b, &t.nchunk_b, &t.nlev_b, &t.chunk_lev_b, &t.lev_nch_b,
+                  &t.wide_b);
     if (e != cudaSuccess) return e;
     e = cudaMalloc(&t.lev_cnt, sizeof(unsigned) * (size_t)(t.nlev_f + t.nlev_b));
     if (e != cudaSuccess) return e;
