@@ -66,6 +66,10 @@ typedef struct tflows_options {
     int block_size;      /* threads per block, 0 = tuned                     */
     int grid_blocks;     /* persistent blocks, 0 = tuned                     */
     int device;          /* CUDA device ordinal, -1 = current                */
+    int inject_stall;    /* test hook: 1 = the first block withholds its
+                            arrival at the first grid barrier, so every
+                            bounded wait runs out and the solve returns
+                            TFLOWS_TIMEOUT (the device stays usable)        */
 } tflows_options;
 
 typedef struct tflows_result {

@@ -93,7 +93,7 @@ class Options(ctypes.Structure):
                 ("ic_sweeps", ctypes.c_int),
                 ("ic_bf16", ctypes.c_int), ("timeout_s", ctypes.c_double),
                 ("block_size", ctypes.c_int), ("grid_blocks", ctypes.c_int),
-                ("device", ctypes.c_int)]
+                ("device", ctypes.c_int), ("inject_stall", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):

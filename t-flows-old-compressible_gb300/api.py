@@ -276,3 +276,36 @@ class Topology:
         if st != OK:
             raise SolverError(st, last_error())
         return grad
+
+
+def solve_batched(topos, vals, bs, xs, methods, precs, maxiters, tols, opts=None,
+                  raise_on_error=True):
+    """All systems in one persistent cooperative launch (tflows_solve_batched_device).
+
+    Lists of equal length: Topology objects (a pattern may repeat), CUDA
+    float64 tensors for values, right-hand sides and solutions (x updated in
+    place), method names or codes, preconditioners, iteration caps and
+    tolerances.  Returns one result record (dict) per system.
+    """
+    n = len(topos)
+    arrs = [vals, bs, xs, methods, precs, maxiters, tols]
+    if any(len(a) != n for a in arrs):
+        raise ValueError("all per-system lists must have the same length")
+    VP = ctypes.c_void_p * n
+    h = VP(*[t.handle.value for t in topos])
+    pv = VP(*[v.data_ptr() for v in vals])
+    pb = VP(*[v.data_ptr() for v in bs])
+    px = VP(*[v.data_ptr() for v in xs])
+    for t in list(vals) + list(bs) + list(xs):
+        if not (t.is_cuda and t.dtype.itemsize == 8 and t.is_contiguous()):
+            raise TypeError("vals, bs, xs must be contiguous CUDA float64 tensors")
+    m = (ctypes.c_int * n)(*[int(METHODS.get(x, x)) for x in methods])
+    pr = (ctypes.c_int * n)(*[int(x) for x in precs])
+    mi = (ctypes.c_int * n)(*[int(x) for x in maxiters])
+    tl = (ctypes.c_double * n)(*[float(x) for x in tols])
+    res = (_native.Result * n)()
+    st = lib().tflows_solve_batched_device(n, h, m, pr, ctypes.byref(opts) if opts else None, pv,
+                                           pb, px, mi, tl, _stream(), res)
+    if raise_on_error and st in (BAD_INPUT, CUDA_ERROR, NO_DEVICE, UNSUPPORTED, TIMEOUT):
+        raise SolverError(st, last_error())
+    return [r.as_dict() for r in res]

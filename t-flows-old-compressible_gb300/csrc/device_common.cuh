@@ -2,7 +2,7 @@
 //
 // * memory-model helpers (relaxed / acquire / release accesses at gpu scope)
 // * a grid barrier for persistent cooperative launches whose every wait is
-//   bounded by %globaltimer and by a shared abort flag
+//   bounded by the SM cycle counter and by a shared abort flag
 // * value-as-flag cells for the sync-free triangular sweeps: a cell holds a
 //   signalling-NaN sentinel until its producer stores the computed value
 //   (arithmetic never yields a signalling NaN, so a stored result can never
@@ -50,11 +50,10 @@ struct DevCtl {
     int pad;
 };
 
-__device__ __forceinline__ long long globaltimer_ns() {
-    long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
+// Wait limits are measured in SM clock cycles (clock64: monotonic and local
+// to the SM, unlike the host-synchronised %globaltimer); the host converts
+// the limit in seconds with the device's highest SM clock, so the real limit
+// is never shorter than requested.
 
 __device__ __forceinline__ long long ld_relaxed_s64(const long long* p) {
     long long v;
@@ -117,10 +116,10 @@ template <> struct Cell<float> {
 };
 
 // Wait until *p holds a produced value.  Bounded: gives up after
-// `timeout_ns` of waiting or when another thread raised the abort flag;
+// `timeout_cyc` of waiting or when another thread raised the abort flag;
 // then returns false (the caller must stop its phase).
 template <typename T>
-__device__ __forceinline__ bool wait_cell(const T* p, T& out, DevCtl* ctl, long long timeout_ns,
+__device__ __forceinline__ bool wait_cell(const T* p, T& out, DevCtl* ctl, long long timeout_cyc,
                                           int where) {
     using C = Cell<T>;
     auto b = C::load(p);
@@ -128,7 +127,7 @@ __device__ __forceinline__ bool wait_cell(const T* p, T& out, DevCtl* ctl, long 
         out = C::value(b);
         return true;
     }
-    long long t0 = globaltimer_ns();
+    long long t0 = clock64();
     unsigned spins = 0;
     while (true) {
         // exponential back-off 32 -> 512 ns keeps many waiting threads from
@@ -141,7 +140,7 @@ __device__ __forceinline__ bool wait_cell(const T* p, T& out, DevCtl* ctl, long 
         }
         if ((++spins & 63u) == 0u) {
             if (ld_relaxed_s32(&ctl->abort)) return false;
-            if (globaltimer_ns() - t0 > timeout_ns) {
+            if (clock64() - t0 > timeout_cyc) {
                 raise_abort(ctl, ST_TIMEOUT, where);
                 return false;
             }
@@ -182,32 +181,45 @@ __device__ __forceinline__ void block_sums(const double (&v)[K], double* sm, dou
 struct Grid {
     DevCtl* ctl;
     double* partials;   // [slots][nblocks]
-    long long timeout_ns;
+    long long timeout_cyc;
     unsigned long long target;  // thread 0 only
     int nblocks;
     int wg;   // global warp index
     int nw;   // warps in the grid
     int lane;
-    int tid;  // global thread index
-    int nt;   // threads in the grid
+    int tid;  // thread index within the group of blocks solving one system
+    int nt;   // threads in the group
+    int bid;  // block index within the group
     unsigned ep_f;  // forward / backward level-sweep epochs (counter targets)
     unsigned ep_b;
+    int stall;      // test hook: block 0 skips its first barrier arrival
 };
 
-__device__ __forceinline__ void grid_init(Grid& g, DevCtl* ctl, double* partials,
-                                          long long timeout_ns) {
+// A "grid" here is the group of `nb` blocks (starting at block `b0` of the
+// launch) that solves one system: barriers, partial sums and work
+// distribution are all relative to the group, so one launch can carry many
+// independent solves.
+__device__ __forceinline__ void grid_init_group(Grid& g, DevCtl* ctl, double* partials,
+                                                long long timeout_cyc, int b0, int nb) {
     g.ctl = ctl;
     g.partials = partials;
-    g.timeout_ns = timeout_ns;
+    g.timeout_cyc = timeout_cyc;
     g.target = 0;
-    g.nblocks = gridDim.x;
+    g.nblocks = nb;
+    g.bid = blockIdx.x - b0;
     g.lane = threadIdx.x & 31;
-    g.tid = blockIdx.x * blockDim.x + threadIdx.x;
-    g.nt = gridDim.x * blockDim.x;
+    g.tid = g.bid * blockDim.x + threadIdx.x;
+    g.nt = nb * blockDim.x;
     g.wg = g.tid >> 5;
     g.nw = g.nt >> 5;
     g.ep_f = 0;
     g.ep_b = 0;
+    g.stall = 0;
+}
+
+__device__ __forceinline__ void grid_init(Grid& g, DevCtl* ctl, double* partials,
+                                          long long timeout_cyc) {
+    grid_init_group(g, ctl, partials, timeout_cyc, 0, gridDim.x);
 }
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -218,16 +230,16 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 
 // Wait (one thread) until *p >= target; bounded like every other wait.
 __device__ __forceinline__ bool wait_count(const unsigned* p, unsigned target, DevCtl* ctl,
-                                           long long timeout_ns, int where) {
+                                           long long timeout_cyc, int where) {
     if (ld_acquire_u32(p) >= target) return true;
-    long long t0 = globaltimer_ns();
+    long long t0 = clock64();
     unsigned spins = 0;
     while (true) {
         __nanosleep(32);
         if (ld_acquire_u32(p) >= target) return true;
         if ((++spins & 127u) == 0u) {
             if (ld_relaxed_s32(&ctl->abort)) return false;
-            if (globaltimer_ns() - t0 > timeout_ns) {
+            if (clock64() - t0 > timeout_cyc) {
                 raise_abort(ctl, ST_TIMEOUT, where);
                 return false;
             }
@@ -244,16 +256,17 @@ __device__ __forceinline__ bool grid_sync(Grid& g, int where) {
     if (threadIdx.x == 0) {
         g.target += (unsigned long long)g.nblocks;
         __threadfence();
-        red_release_add_u64(&g.ctl->bar, 1ull);
+        if (g.stall && g.bid == 0) g.stall = 0;  // withheld: the barrier cannot complete
+        else red_release_add_u64(&g.ctl->bar, 1ull);
         int ok = 1;
         long long t0 = 0;
         unsigned spins = 0;
         while (ld_acquire_u64(&g.ctl->bar) < g.target) {
             if ((++spins & 255u) == 0u) {
                 if (ld_relaxed_s32(&g.ctl->abort)) { ok = 0; break; }
-                long long t = globaltimer_ns();
+                long long t = clock64();
                 if (t0 == 0) t0 = t;
-                else if (t - t0 > g.timeout_ns) {
+                else if (t - t0 > g.timeout_cyc) {
                     raise_abort(g.ctl, ST_TIMEOUT, where);
                     ok = 0;
                     break;
@@ -276,7 +289,7 @@ __device__ __forceinline__ void publish(Grid& g, int slot, const double (&v)[K])
     block_sums<K>(v, sm, out);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) g.partials[(size_t)(slot + k) * g.nblocks + blockIdx.x] = out[k];
+        for (int k = 0; k < K; ++k) g.partials[(size_t)(slot + k) * g.nblocks + g.bid] = out[k];
     }
 }
 

@@ -73,6 +73,7 @@ struct SolveRequest {
     int max_refinements = 30;
     int ic_sweeps = 0;
     int refine_restart = 0;
+    int inject_stall = 0;
     double timeout_s = 5.0;
     int block = 0;
     int grid = 0;
@@ -91,6 +92,16 @@ struct SolveReport {
     std::string message;
 };
 
+// One system of a batched launch.
+struct BatchSpec {
+    const DeviceTopology* t;
+    Workspace* ws;
+    SolveRequest rq;
+    double* x;  // workspace x (slot 11), in/out
+    double* r;  // workspace residual (slot 12), holds b on entry
+    SolveReport* rep;
+};
+
 // krylov.cu
 cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t);
 void free_workspace(Workspace& ws);
@@ -104,6 +115,8 @@ int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, do
 int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, double timeout_s,
               cudaStream_t s, SolveReport& rep);
 // r <- r - A x (Resid), device arrays.
+// All systems in one cooperative launch (block groups sized by expected work).
+int run_batch(std::vector<BatchSpec>& specs, cudaStream_t s, double* seconds);
 cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, double* r,
                       cudaStream_t s);
 cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, double* y, bool fp32,

@@ -26,8 +26,9 @@ struct KParams {
     DevCtl* ctl;
     DevState* state;
     double* partials;
-    long long timeout_ns;
+    long long timeout_cyc;
     int mode;  // 0 solve, 1 Prec1 only
+    int stall;
 };
 
 __device__ int status_of(const SolveOut& o, const DevCtl* ctl) {
@@ -44,7 +45,8 @@ __device__ int status_of(const SolveOut& o, const DevCtl* ctl) {
 template <typename T, int METHOD>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) krylov_kernel(KParams<T> P) {
     Grid g;
-    grid_init(g, P.ctl, P.partials, P.timeout_ns);
+    grid_init(g, P.ctl, P.partials, P.timeout_cyc);
+    g.stall = P.stall;
     SolveOut out;
     out.exit_kind = 0;
     out.iterations = 0;
@@ -84,14 +86,16 @@ struct MixedParams {
     DevCtl* ctl;
     DevState* state;
     double* partials;
-    long long timeout_ns;
+    long long timeout_cyc;
+    int stall;
 };
 
 // KIND: 0 restarted CG, 2 restarted CGS, 1 CG with reliable updates.
 template <int KIND>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) mixed_kernel(MixedParams P) {
     Grid g;
-    grid_init(g, P.ctl, P.partials, P.timeout_ns);
+    grid_init(g, P.ctl, P.partials, P.timeout_cyc);
+    g.stall = P.stall;
     MixedOut out;
     out.exit_kind = 0;
     out.iterations = 0;
@@ -195,6 +199,18 @@ __global__ void pattern_outer_kernel(int n, const int* __restrict__ rowptr,
         const double li = lam[i];
         for (int j = rowptr[i]; j < rowptr[i + 1]; ++j) g[j] = -li * x[col[j]];
     }
+}
+
+// Wait limit in SM cycles for `sec` seconds at the device's highest clock.
+long long timeout_cycles(double sec) {
+    static int khz = 0;
+    if (khz == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev);
+        if (khz <= 0) khz = 2100000;
+    }
+    return (long long)(sec * (double)khz * 1e3);
 }
 
 int g_num_sms = 0;
@@ -352,7 +368,7 @@ int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, doubl
     P.ctl = (DevCtl*)ws.ctl;
     P.state = (DevState*)ws.state;
     P.partials = ws.partials;
-    P.timeout_ns = (long long)(timeout_s * 1e9);
+    P.timeout_cyc = timeout_cycles(timeout_s);
     P.mode = 1;
     cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
     reset_counters(t, s);
@@ -378,18 +394,48 @@ int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, doubl
 
 namespace {
 
-int run_mixed(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
-              cudaStream_t s, SolveReport& rep) {
-    MixedParams P;
+// Parameters of one FP64 (reference arithmetic) solve; queues the control
+// block / counter resets and the IC sentinel fill on stream s.
+cudaError_t prepare_fp64(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x,
+                         double* r, cudaStream_t s, KParams<double>& P) {
+    std::memset(&P, 0, sizeof(P));
+    P.m = make_mat<double>(t, ws.sval64);
+    P.v = carve<double>(ws.vec64, ws.vec_cap, x, r);
+    P.cfg.method = rq.method == 2 ? 2 : 0;
+    P.cfg.prec = rq.prec;
+    P.cfg.maxiter = rq.maxiter;
+    P.cfg.tol = rq.tol;
+    P.cfg.x_is_zero = rq.x_is_zero;
+    P.cfg.do_prec1 = 1;
+    P.cfg.tol_is_relative = rq.tol_relative;
+    P.ctl = (DevCtl*)ws.ctl;
+    P.state = (DevState*)ws.state;
+    P.partials = ws.partials;
+    P.timeout_cyc = timeout_cycles(rq.timeout_s);
+    P.mode = 0;
+    P.stall = rq.inject_stall;
+    cudaError_t e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
+    reset_counters(t, s);
+    if (rq.prec == 2) {
+        const long long nvec = (long long)t.nslices * kWarp;
+        fill_sentinel_kernel<double>
+            <<<std::min(1024, (int)((nvec + 255) / 256)), 256, 0, s>>>(P.v.w, nvec);
+    }
+    return e;
+}
+
+// Parameters of one mixed-precision solve.  b is kept in FP64 workspace slot
+// 13 (the residual slot r is rewritten by every refinement).
+cudaError_t prepare_mixed(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x,
+                          double* r, cudaStream_t s, MixedParams& P) {
     std::memset(&P, 0, sizeof(P));
     P.m64 = make_mat<double>(t, ws.sval64);
     P.m32 = make_mat<float>(t, ws.sval32);
     P.x64 = x;
     P.r64 = r;
-    // b is kept in the FP64 workspace slot 13 (the residual slot r is
-    // rewritten by every refinement).
     double* b64 = ws.vec64 + 13 * ws.vec_cap;
-    cudaError_t e = cudaMemcpyAsync(b64, r, sizeof(double) * t.n, cudaMemcpyDeviceToDevice, s);
+    cudaError_t e = cudaSuccess;
+    if (b64 != r) e = cudaMemcpyAsync(b64, r, sizeof(double) * t.n, cudaMemcpyDeviceToDevice, s);
     P.b64 = b64;
     P.D64 = ws.vec64 + 4 * ws.vec_cap;
     P.xbest = ws.vec64;
@@ -407,24 +453,33 @@ int run_mixed(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, do
     P.ctl = (DevCtl*)ws.ctl;
     P.state = (DevState*)ws.state;
     P.partials = ws.partials;
-    P.timeout_ns = (long long)(rq.timeout_s * 1e9);
+    P.timeout_cyc = timeout_cycles(rq.timeout_s);
+    P.stall = rq.inject_stall;
     if (e == cudaSuccess) e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
     reset_counters(t, s);
-    auto kern = P.cfg.method == 2 ? mixed_kernel<2> : (P.cfg.restart ? mixed_kernel<0> : mixed_kernel<1>);
-    const int grid = choose_grid(t, rq.grid, max_coresident(kern, kBlock));
-    cudaEventRecord(ws.ev0, s);
-    if (e == cudaSuccess) e = launch_coop(kern, P, grid, s);
-    cudaEventRecord(ws.ev1, s);
-    DevState st;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ws.state, sizeof(st), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        rep.status = ST_CUDA_ERROR;
-        rep.message = std::string("mixed solver: ") + cudaGetErrorString(e);
-        return rep.status;
+    return e;
+}
+
+// Algorithmic bytes of a finished solve (values + indices of each product,
+// each row's x gathered once, plus the vector passes of the schedule).
+double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevState& st) {
+    const double sl = 8.0 * (t.nslices + 1);
+    const double spmv64 = (double)t.nnz * 12.0 + sl + 16.0 * t.n;
+    const bool cgs = rq.method == 2;
+    if (rq.precision == 1) {
+        const double spmv32 = (double)t.nnz * 8.0 + sl + 8.0 * t.n;
+        const double inner_it = cgs ? 2 * spmv32 + 4.0 * t.n * 22
+                                    : spmv32 + 4.0 * t.n * (rq.prec == 1 ? 12 : 10);
+        return inner_it * st.inner_iters + (spmv64 + 8.0 * t.n * 4) * (st.refinements + 1);
     }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, ws.ev0, ws.ev1);
+    const int it = std::max(0, std::min(st.iterations, rq.maxiter));
+    const double per_it = cgs ? 2 * spmv64 + 8.0 * t.n * 22
+                              : spmv64 + 8.0 * t.n * (rq.prec == 1 ? 12 : 10);
+    return per_it * it + spmv64 + 8.0 * t.n * 4;
+}
+
+void fill_report(const DeviceTopology& t, const SolveRequest& rq, const DevState& st, double sec,
+                 SolveReport& rep) {
     rep.status = st.status;
     rep.exit_kind = st.exit_kind;
     rep.iterations = st.iterations;
@@ -432,57 +487,21 @@ int run_mixed(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, do
     rep.refinements = st.refinements;
     rep.ini_res = st.ini_res;
     rep.fin_res = st.fin_res;
-    rep.seconds = ms * 1e-3;
-    const double sl = 8.0 * (t.nslices + 1);
-    const double spmv32 = (double)t.nnz * 8.0 + sl + 8.0 * t.n;
-    const double spmv64 = (double)t.nnz * 12.0 + sl + 16.0 * t.n;
-    const double inner_it = P.cfg.method == 2 ? 2 * spmv32 + 4.0 * t.n * 22
-                                              : spmv32 + 4.0 * t.n * (rq.prec == 1 ? 12 : 10);
-    rep.bytes = inner_it * st.inner_iters + (spmv64 + 8.0 * t.n * 4) * (st.refinements + 1);
+    rep.seconds = sec;
+    rep.bytes = solve_bytes(t, rq, st);
     if (st.status == ST_TIMEOUT)
         rep.message = "device wait exceeded the timeout (site " + std::to_string(st.timeout_where) + ")";
-    return rep.status;
 }
 
-}  // namespace
-
-int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
-              cudaStream_t s, SolveReport& rep) {
-    if (rq.precision == 1) return run_mixed(t, ws, rq, x, r, s, rep);
-    KParams<double> P;
-    std::memset(&P, 0, sizeof(P));
-    P.m = make_mat<double>(t, ws.sval64);
-    P.v = carve<double>(ws.vec64, ws.vec_cap, x, r);
-    P.cfg.method = rq.method == 2 ? 2 : 0;
-    P.cfg.prec = rq.prec;
-    P.cfg.maxiter = rq.maxiter;
-    P.cfg.tol = rq.tol;
-    P.cfg.x_is_zero = rq.x_is_zero;
-    P.cfg.do_prec1 = 1;
-    P.cfg.tol_is_relative = rq.tol_relative;
-    P.ctl = (DevCtl*)ws.ctl;
-    P.state = (DevState*)ws.state;
-    P.partials = ws.partials;
-    P.timeout_ns = (long long)(rq.timeout_s * 1e9);
-    P.mode = 0;
-    cudaError_t e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
-    reset_counters(t, s);
-    if (rq.prec == 2) {
-        const long long nvec = (long long)t.nslices * kWarp;
-        fill_sentinel_kernel<double><<<std::min(1024, (int)((nvec + 255) / 256)), 256, 0, s>>>(P.v.w, nvec);
-    }
-    auto kern = P.cfg.method == 2 ? krylov_kernel<double, 2> : krylov_kernel<double, 0>;
+template <typename K, typename P>
+int launch_and_report(K kern, P& params, const DeviceTopology& t, Workspace& ws,
+                      const SolveRequest& rq, cudaStream_t s, SolveReport& rep, cudaError_t e) {
     const int grid = choose_grid(t, rq.grid, max_coresident(kern, kBlock));
     cudaEventRecord(ws.ev0, s);
-    if (e == cudaSuccess) e = launch_coop(kern, P, grid, s);
+    if (e == cudaSuccess) e = launch_coop(kern, params, grid, s);
     cudaEventRecord(ws.ev1, s);
-    if (e != cudaSuccess) {
-        rep.status = ST_CUDA_ERROR;
-        rep.message = std::string("solver launch: ") + cudaGetErrorString(e);
-        return rep.status;
-    }
     DevState st;
-    e = cudaMemcpyAsync(&st, ws.state, sizeof(st), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ws.state, sizeof(st), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         rep.status = ST_CUDA_ERROR;
@@ -491,23 +510,189 @@ int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, do
     }
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ws.ev0, ws.ev1);
-    rep.status = st.status;
-    rep.exit_kind = st.exit_kind;
-    rep.iterations = st.iterations;
-    rep.ini_res = st.ini_res;
-    rep.fin_res = st.fin_res;
-    rep.seconds = ms * 1e-3;
-    // Algorithmic bytes: per iteration one SELL product (values + indices,
-    // each row's x gathered once) plus the vector passes of the schedule.
-    const double spmv = (double)t.nnz * (8.0 + 4.0) + 8.0 * (t.nslices + 1) + 16.0 * t.n;
-    const int it = std::max(0, std::min(st.iterations, rq.maxiter));
-    double per_it;
-    if (P.cfg.method == 2) per_it = 2 * spmv + 8.0 * t.n * 22;
-    else per_it = spmv + 8.0 * t.n * (rq.prec == 1 ? 12 : 10);
-    rep.bytes = per_it * it + spmv + 8.0 * t.n * 4;
-    if (st.status == ST_TIMEOUT)
-        rep.message = "device wait exceeded the timeout (site " + std::to_string(st.timeout_where) + ")";
+    fill_report(t, rq, st, ms * 1e-3, rep);
     return rep.status;
+}
+
+// ---- batched solves: one cooperative launch, one block group per system ------
+struct BatchItem {
+    int b0;       // first block of the group
+    int nb;       // blocks in the group
+    int mixed;    // 0: FP64 params, 1: mixed params
+    int method;   // 0 CG, 2 CGS
+    KParams<double> P64;
+    MixedParams PM;
+};
+
+template <int MIXED>
+__global__ void __launch_bounds__(kBlock, kMinBlocks)
+    batch_kernel(const BatchItem* __restrict__ items, const int* __restrict__ block_item) {
+    const BatchItem& it = items[block_item[blockIdx.x]];
+    Grid g;
+    if (!MIXED) {
+        KParams<double> P = it.P64;
+        grid_init_group(g, P.ctl, P.partials, P.timeout_cyc, it.b0, it.nb);
+        SolveOut out;
+        out.exit_kind = 0;
+        out.iterations = 0;
+        out.ini_res = 0.0;
+        out.fin_res = 0.0;
+        out.bnrm2 = 0.0;
+        if (it.method == 2) cgs_solve(g, P.m, P.v, P.cfg, out);
+        else cg_solve(g, P.m, P.v, P.cfg, out);
+        if (g.bid == 0 && threadIdx.x == 0) {
+            DevState* s = P.state;
+            s->status = status_of(out, P.ctl);
+            s->exit_kind = out.exit_kind;
+            s->iterations = out.iterations;
+            s->ini_res = out.ini_res;
+            s->fin_res = out.fin_res;
+            s->bnrm2 = out.bnrm2;
+            s->timeout_where = P.ctl->where;
+        }
+    } else {
+        MixedParams P = it.PM;
+        grid_init_group(g, P.ctl, P.partials, P.timeout_cyc, it.b0, it.nb);
+        MixedOut out;
+        out.exit_kind = 0;
+        out.iterations = 0;
+        out.refinements = 0;
+        out.ini_res = 0.0;
+        out.fin_res = 0.0;
+        out.bnrm2 = 0.0;
+        mixed_solve(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.v32, P.cfg, out);
+        if (g.bid == 0 && threadIdx.x == 0) {
+            DevState* s = P.state;
+            SolveOut o;
+            o.exit_kind = out.exit_kind;
+            o.fin_res = out.fin_res;
+            s->status = status_of(o, P.ctl);
+            s->exit_kind = out.exit_kind;
+            s->iterations = out.iterations;
+            s->inner_iters = out.iterations;
+            s->refinements = out.refinements;
+            s->ini_res = out.ini_res;
+            s->fin_res = out.fin_res;
+            s->bnrm2 = out.bnrm2;
+            s->timeout_where = P.ctl->where;
+        }
+    }
+}
+
+}  // namespace
+
+int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
+              cudaStream_t s, SolveReport& rep) {
+    if (rq.precision == 1) {
+        MixedParams P;
+        cudaError_t e = prepare_mixed(t, ws, rq, x, r, s, P);
+        auto kern = P.cfg.method == 2 ? mixed_kernel<2>
+                                      : (P.cfg.restart ? mixed_kernel<0> : mixed_kernel<1>);
+        return launch_and_report(kern, P, t, ws, rq, s, rep, e);
+    }
+    KParams<double> P;
+    cudaError_t e = prepare_fp64(t, ws, rq, x, r, s, P);
+    auto kern = P.cfg.method == 2 ? krylov_kernel<double, 2> : krylov_kernel<double, 0>;
+    return launch_and_report(kern, P, t, ws, rq, s, rep, e);
+}
+
+int run_batch(std::vector<BatchSpec>& specs, cudaStream_t s, double* seconds) {
+    const int count = (int)specs.size();
+    if (count == 0) return ST_OK;
+    const bool mixed = specs[0].rq.precision == 1;
+    for (auto& sp : specs)
+        if ((sp.rq.precision == 1) != mixed) {
+            for (auto& q : specs) {
+                q.rep->status = ST_BAD_INPUT;
+                q.rep->message = "one precision per batched launch";
+            }
+            return ST_BAD_INPUT;
+        }
+    auto kern = mixed ? batch_kernel<1> : batch_kernel<0>;
+    const int maxb = max_coresident(kern, kBlock);
+    if (count > maxb) {
+        for (auto& sp : specs) {
+            sp.rep->status = ST_BAD_INPUT;
+            sp.rep->message = "more systems than co-resident blocks (" + std::to_string(maxb) + ")";
+        }
+        return ST_BAD_INPUT;
+    }
+    // Blocks per system in proportion to the expected work, N^(4/3) (rows
+    // times a CG iteration count growing like the mesh edge), at least one,
+    // at most one block per 8 slices.
+    std::vector<double> w(count);
+    double wsum = 0.0;
+    for (int k = 0; k < count; ++k) {
+        w[k] = std::pow((double)specs[k].t->n, 4.0 / 3.0);
+        wsum += w[k];
+    }
+    std::vector<int> nb(count);
+    int total = 0;
+    for (int k = 0; k < count; ++k) {
+        const int cap = std::max(1, blocks_for(specs[k].t->nslices));
+        nb[k] = std::max(1, std::min(cap, (int)std::floor((maxb - count) * w[k] / wsum) + 1));
+        total += nb[k];
+    }
+    while (total > maxb) {
+        int big = (int)(std::max_element(nb.begin(), nb.end()) - nb.begin());
+        --nb[big];
+        --total;
+    }
+    std::vector<BatchItem> items(count);
+    std::vector<int> block_item(total);
+    cudaError_t e = cudaSuccess;
+    int b0 = 0;
+    for (int k = 0; k < count; ++k) {
+        BatchSpec& sp = specs[k];
+        BatchItem& it = items[k];
+        std::memset(&it, 0, sizeof(it));
+        it.b0 = b0;
+        it.nb = nb[k];
+        it.method = sp.rq.method == 2 ? 2 : 0;
+        it.mixed = sp.rq.precision == 1;
+        cudaError_t ek = it.mixed ? prepare_mixed(*sp.t, *sp.ws, sp.rq, sp.x, sp.r, s, it.PM)
+                                  : prepare_fp64(*sp.t, *sp.ws, sp.rq, sp.x, sp.r, s, it.P64);
+        if (ek != cudaSuccess) e = ek;
+        for (int j = 0; j < nb[k]; ++j) block_item[b0 + j] = k;
+        b0 += nb[k];
+    }
+    BatchItem* d_items = nullptr;
+    int* d_map = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_items, sizeof(BatchItem) * count, s);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_map, sizeof(int) * total, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_items, items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_map, block_item.data(), sizeof(int) * total, cudaMemcpyHostToDevice, s);
+    cudaEvent_t e0 = specs[0].ws->ev0, e1 = specs[0].ws->ev1;
+    cudaEventRecord(e0, s);
+    if (e == cudaSuccess) {
+        void* args[] = {&d_items, &d_map};
+        e = cudaLaunchCooperativeKernel((const void*)kern, dim3(total), dim3(kBlock), args, 0, s);
+    }
+    cudaEventRecord(e1, s);
+    std::vector<DevState> st(count);
+    for (int k = 0; k < count && e == cudaSuccess; ++k)
+        e = cudaMemcpyAsync(&st[k], specs[k].ws->state, sizeof(DevState), cudaMemcpyDeviceToHost, s);
+    if (d_items) cudaFreeAsync(d_items, s);
+    if (d_map) cudaFreeAsync(d_map, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        for (auto& sp : specs) {
+            sp.rep->status = ST_CUDA_ERROR;
+            sp.rep->message = std::string("batched solver: ") + cudaGetErrorString(e);
+        }
+        return ST_CUDA_ERROR;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (seconds) *seconds = ms * 1e-3;
+    int worst = ST_OK;
+    for (int k = 0; k < count; ++k) {
+        fill_report(*specs[k].t, specs[k].rq, st[k], ms * 1e-3, *specs[k].rep);
+        worst = std::max(worst, st[k].status);
+    }
+    return worst;
 }
 
 cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, double* r,

@@ -264,7 +264,7 @@ __device__ __forceinline__ bool sweep_chunk(const Grid& g, const Mat<T>& m, int 
     }
     int cursor = t0;
     bool done = row < 0;
-    const long long start = globaltimer_ns();
+    const long long start = clock64();
     unsigned spins = 0;
     while (true) {
         if (!done) {
@@ -310,7 +310,7 @@ __device__ __forceinline__ bool sweep_chunk(const Grid& g, const Mat<T>& m, int 
             __nanosleep(min((unsigned)TFLOWS_SWEEP_SLEEP, 8u << min(spins - 4u, 10u)));
         if ((spins & 63u) == 0u) {
             bool quit = ld_relaxed_s32(&g.ctl->abort) != 0;
-            if (!quit && globaltimer_ns() - start > g.timeout_ns) {
+            if (!quit && clock64() - start > g.timeout_cyc) {
                 raise_abort(g.ctl, ST_TIMEOUT, where);
                 quit = true;
             }

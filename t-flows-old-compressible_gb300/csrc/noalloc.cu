@@ -46,7 +46,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 struct NaParams {
     int n, prec, maxiter;
     double tol;
-    long long timeout_ns;
+    long long timeout_cyc;
     const int* rowptr;
     const int* col;
     const int* diag;
@@ -64,14 +64,7 @@ struct NaParams {
 // per row, same per-row operation order as the reference loops.
 __global__ void __launch_bounds__(kNaBlock) noalloc_cg_kernel(NaParams P) {
     Grid g;
-    g.ctl = P.ctl;
-    g.partials = P.partials;
-    g.timeout_ns = P.timeout_ns;
-    g.target = 0;
-    g.nblocks = gridDim.x;
-    g.lane = threadIdx.x & 31;
-    g.wg = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    g.nw = (int)((gridDim.x * blockDim.x) >> 5);
+    grid_init(g, P.ctl, P.partials, P.timeout_cyc);
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int nt = gridDim.x * blockDim.x;
     const int n = P.n;
@@ -236,7 +229,9 @@ extern "C" int tflows_cg_noalloc(int n, const int* rowptr, const int* col, const
     P.prec = prec;
     P.maxiter = maxiter;
     P.tol = tol;
-    P.timeout_ns = 5000000000LL;
+    int khz = 0;
+    cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev);
+    P.timeout_cyc = 5LL * (khz > 0 ? khz : 2100000) * 1000LL;  // 5 s of SM cycles
     P.rowptr = rowptr;
     P.col = col;
     P.diag = diag;

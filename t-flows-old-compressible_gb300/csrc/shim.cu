@@ -21,6 +21,8 @@
 struct tflows_topology {
     tflows::DeviceTopology t;
     tflows::Workspace ws;
+    // extra workspaces for batches that solve several systems on this pattern
+    std::vector<std::unique_ptr<tflows::Workspace>> extra_ws;
     std::mutex mu;
     // cache key (legacy host path)
     const void* k_acol = nullptr;
@@ -296,6 +298,8 @@ void destroy_topo(tflows_topology* tp) {
     if (!tp) return;
     free_topology_arrays(tp->t);
     free_workspace(tp->ws);
+    for (auto& w : tp->extra_ws) free_workspace(*w);
+    tp->extra_ws.clear();
 }
 
 struct TopoDeleter {
@@ -368,6 +372,7 @@ SolveRequest make_request(const tflows_options& o, int method, int prec, int max
     rq.max_refinements = o.max_refinements;
     rq.ic_sweeps = o.ic_sweeps;
     rq.refine_restart = o.refine_restart;
+    rq.inject_stall = o.inject_stall;
     rq.timeout_s = o.timeout_s > 0 ? o.timeout_s : 5.0;
     rq.block = o.block_size;
     rq.grid = o.grid_blocks;
@@ -733,17 +738,77 @@ int tflows_solve_batched_device(int count, tflows_topology* const* topos, const 
                                 const double* const* vals, const double* const* bs,
                                 double* const* xs, const int* maxiters, const double* tols,
                                 void* stream, tflows_result* results) {
+    t_error.clear();
     if (count < 0 || (count > 0 && (!topos || !methods || !precs || !vals || !bs || !xs || !maxiters ||
                                     !tols)))
         return fail(TFLOWS_BAD_INPUT, "null argument");
-    int worst = TFLOWS_OK;
+    if (count == 0) return TFLOWS_OK;
+    for (int k = 0; k < count; ++k)
+        if (!topos[k] || !vals[k] || !bs[k] || !xs[k]) return fail(TFLOWS_BAD_INPUT, "null system");
+    tflows_options o;
+    if (opt) o = *opt;
+    else default_opts(&o);
+    std::vector<tflows_topology*> uniq(topos, topos + count);
+    std::sort(uniq.begin(), uniq.end());
+    uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+    std::vector<std::unique_lock<std::mutex>> locks;
+    for (auto* tp : uniq) locks.emplace_back(tp->mu);
+    const int dev = topos[0]->t.device;
+    for (auto* tp : uniq)
+        if (tp->t.device != dev) return fail(TFLOWS_BAD_INPUT, "systems on different devices");
+    cudaSetDevice(dev);
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<SolveReport> reps(count);
+    std::vector<BatchSpec> specs(count);
+    std::vector<std::pair<tflows_topology*, int>> uses;
     for (int k = 0; k < count; ++k) {
-        int st = tflows_solve_device(topos[k], methods[k], precs[k], opt, vals[k], bs[k], xs[k],
-                                     nullptr, maxiters[k], tols[k], stream,
-                                     results ? results + k : nullptr);
-        if (st > worst) worst = st;
+        tflows_topology* tp = topos[k];
+        int j = 0;
+        for (auto& u : uses)
+            if (u.first == tp) j = ++u.second;
+        if (j == 0) uses.emplace_back(tp, 0);
+        while ((int)tp->extra_ws.size() < j) tp->extra_ws.emplace_back(new Workspace());
+        Workspace* ws = j == 0 ? &tp->ws : tp->extra_ws[j - 1].get();
+        SolveRequest rq = make_request(o, methods[k], precs[k], maxiters[k], tols[k]);
+        if (rq.method == TFLOWS_METHOD_BICG_TRUE)
+            return fail(TFLOWS_UNSUPPORTED, "true BiCG is not available in batched solves");
+        if (rq.prec == 2) {
+            if (!tp->t.ic_ok) return fail(TFLOWS_BAD_INPUT, "IC(0) needs a triangular-ordered pattern");
+            cudaError_t e = build_levels(tp->t);
+            if (e != cudaSuccess) return cuda_fail(e, "level sets");
+        }
+        cudaError_t e = ensure_workspace(*ws, tp->t);
+        if (e == cudaSuccess) e = permute_values(tp->t, *ws, vals[k], true, rq.precision != TFLOWS_FP64, s);
+        double* X = ws->vec64 + 11 * ws->vec_cap;
+        double* R = ws->vec64 + 12 * ws->vec_cap;
+        const size_t nb = sizeof(double) * tp->t.n;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(X, xs[k], nb, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(R, bs[k], nb, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return cuda_fail(e, "batch staging");
+        specs[k] = BatchSpec{&tp->t, ws, rq, X, R, &reps[k]};
     }
+    double sec = 0.0;
+    int worst = run_batch(specs, s, &sec);
+    std::string msg;
+    for (int k = 0; k < count; ++k)
+        if (!reps[k].message.empty()) {
+            msg = "system " + std::to_string(k) + ": " + reps[k].message;
+            break;
+        }
+    if (worst == TFLOWS_CUDA_ERROR || worst == TFLOWS_BAD_INPUT) {
+        for (int k = 0; k < count; ++k) record(reps[k], results ? results + k : nullptr);
+        return fail(worst, msg);
+    }
+    t_error = msg;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < count && e == cudaSuccess; ++k)
+        e = cudaMemcpyAsync(xs[k], specs[k].x, sizeof(double) * specs[k].t->n,
+                            cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "batch results");
+    for (int k = 0; k < count; ++k) record(reps[k], results ? results + k : nullptr);
     t_status = worst;
+    t_error = msg;
     return worst;
 }
 
