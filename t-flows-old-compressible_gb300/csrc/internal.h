@@ -20,6 +20,7 @@ struct DeviceTopology {
     int max_len = 0;
     bool ic_ok = false;        // lower part = slots before the diagonal, ascending
     bool levels_built = false;
+    bool tsym = false;         // every entry has its transpose (valid once tpos exists)
     int nlev_f = 0, nlev_b = 0;
     int nchunk_f = 0, nchunk_b = 0;
     int wide_f = 0, wide_b = 0;  // chunks in the widest level
@@ -49,6 +50,7 @@ struct Workspace {
     int part_cap = 0;          // blocks
     double* sval64 = nullptr;
     float* sval32 = nullptr;
+    double* svalT64 = nullptr;  // A^T values (true BiCG), allocated on first use
     double* vec64 = nullptr;   // kVecs vectors of vec_cap doubles
     float* vec32 = nullptr;    // kVecs vectors of vec_cap floats
     double* csr_val = nullptr; // staging for host values (nnz)
@@ -108,6 +110,9 @@ void free_workspace(Workspace& ws);
 // Values (nnz FP64, stored order, device) -> SELL values (FP64 and/or FP32).
 cudaError_t permute_values(const DeviceTopology& t, Workspace& ws, const double* csr_val,
                            bool want64, bool want32, cudaStream_t s);
+// A^T values in A's pattern into ws.svalT64 (needs t.tpos).
+cudaError_t permute_transposed(const DeviceTopology& t, Workspace& ws, const double* csr_val,
+                               cudaStream_t s);
 // Runs a full solve. x (n) and r (n, holds b on entry) are device FP64 arrays.
 int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
               cudaStream_t s, SolveReport& rep);

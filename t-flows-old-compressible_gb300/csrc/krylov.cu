@@ -21,6 +21,7 @@ constexpr int kMinBlocks = TFLOWS_MINBLOCKS;
 template <typename T>
 struct KParams {
     Mat<T> m;
+    Mat<T> mT;  // A^T values in A's pattern (true BiCG only)
     Vecs<T> v;
     SolveCfg cfg;
     DevCtl* ctl;
@@ -58,6 +59,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) krylov_kernel(KParams<T> P
         out.exit_kind = ok ? EXIT_CONVERGED : EXIT_ABORT;
     } else if (METHOD == 2) {
         cgs_solve(g, P.m, P.v, P.cfg, out);
+    } else if (METHOD == 3) {
+        bicg_true_solve(g, P.m, P.mT, P.v, P.cfg, out);
     } else {
         cg_solve(g, P.m, P.v, P.cfg, out);
     }
@@ -149,15 +152,17 @@ __global__ void to_double_kernel(const float* __restrict__ a, double* __restrict
         b[i] = (double)a[i];
 }
 
-// SELL values from stored-order values: one thread per row.
+// SELL values from stored-order values: one thread per row.  With `tpos`
+// the values of A^T in A's pattern (entry (i,j) <- stored entry (j,i)).
 __global__ void permute_kernel(int n, const int* __restrict__ rowptr,
                                const long long* __restrict__ soff, const double* __restrict__ val,
-                               double* __restrict__ s64, float* __restrict__ s32) {
+                               double* __restrict__ s64, float* __restrict__ s32,
+                               const int* __restrict__ tpos) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int b = rowptr[i], e = rowptr[i + 1];
         const long long base = soff[i >> 5] + (i & 31);
         for (int j = b; j < e; ++j) {
-            const double a = val[j];
+            const double a = tpos ? val[tpos[j]] : val[j];
             const long long o = base + 32LL * (j - b);
             if (s64) s64[o] = a;
             if (s32) s32[o] = (float)a;
@@ -272,8 +277,10 @@ cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t) {
     if (sl > ws.sell_cap) {
         if (ws.sval64) cudaFree(ws.sval64);
         if (ws.sval32) cudaFree(ws.sval32);
+        if (ws.svalT64) cudaFree(ws.svalT64);
         ws.sval64 = nullptr;
         ws.sval32 = nullptr;
+        ws.svalT64 = nullptr;
         if ((e = cudaMalloc(&ws.sval64, sl * sizeof(double))) != cudaSuccess) return e;
         if ((e = cudaMalloc(&ws.sval32, sl * sizeof(float))) != cudaSuccess) return e;
         ws.sell_cap = sl;
@@ -301,7 +308,7 @@ cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t) {
 
 void free_workspace(Workspace& ws) {
     for (void* p : {(void*)ws.sval64, (void*)ws.sval32, (void*)ws.vec64, (void*)ws.vec32,
-                    (void*)ws.csr_val, (void*)ws.partials, ws.ctl, ws.state})
+                    (void*)ws.csr_val, (void*)ws.partials, ws.ctl, ws.state, (void*)ws.svalT64})
         if (p) cudaFree(p);
     if (ws.ev0) cudaEventDestroy(ws.ev0);
     if (ws.ev1) cudaEventDestroy(ws.ev1);
@@ -312,7 +319,19 @@ cudaError_t permute_values(const DeviceTopology& t, Workspace& ws, const double*
                            bool want64, bool want32, cudaStream_t s) {
     const int nb = std::min(std::max(1, (t.n + 255) / 256), sms() * 16);
     permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.soff, csr_val, want64 ? ws.sval64 : nullptr,
-                                      want32 ? ws.sval32 : nullptr);
+                                      want32 ? ws.sval32 : nullptr, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t permute_transposed(const DeviceTopology& t, Workspace& ws, const double* csr_val,
+                               cudaStream_t s) {
+    if (!t.tpos) return cudaErrorInvalidValue;
+    if (!ws.svalT64) {
+        cudaError_t e = cudaMalloc(&ws.svalT64, std::max<size_t>(ws.sell_cap, 1) * sizeof(double));
+        if (e != cudaSuccess) return e;
+    }
+    const int nb = std::min(std::max(1, (t.n + 255) / 256), sms() * 16);
+    permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.soff, csr_val, ws.svalT64, nullptr, t.tpos);
     return cudaGetLastError();
 }
 
@@ -401,7 +420,8 @@ cudaError_t prepare_fp64(const DeviceTopology& t, Workspace& ws, const SolveRequ
     std::memset(&P, 0, sizeof(P));
     P.m = make_mat<double>(t, ws.sval64);
     P.v = carve<double>(ws.vec64, ws.vec_cap, x, r);
-    P.cfg.method = rq.method == 2 ? 2 : 0;
+    P.cfg.method = rq.method == 2 || rq.method == 3 ? rq.method : 0;
+    if (rq.method == 3) P.mT = make_mat<double>(t, ws.svalT64);
     P.cfg.prec = rq.prec;
     P.cfg.maxiter = rq.maxiter;
     P.cfg.tol = rq.tol;
@@ -592,7 +612,9 @@ int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, do
     }
     KParams<double> P;
     cudaError_t e = prepare_fp64(t, ws, rq, x, r, s, P);
-    auto kern = P.cfg.method == 2 ? krylov_kernel<double, 2> : krylov_kernel<double, 0>;
+    auto kern = P.cfg.method == 2   ? krylov_kernel<double, 2>
+                : P.cfg.method == 3 ? krylov_kernel<double, 3>
+                                    : krylov_kernel<double, 0>;
     return launch_and_report(kern, P, t, ws, rq, s, rep, e);
 }
 

@@ -718,6 +718,123 @@ __device__ void cgs_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& 
     out.iterations = iter;
 }
 
+// ---- BiCG with the transposed shadow sequence (extension) ---------------------
+// The textbook preconditioned BiCG (the shadow residual is multiplied by A^T,
+// whose values mT holds in A's pattern), for nonsymmetric systems where the
+// reference's "bicg" (shadow multiplied by A, i.e. CG) may fail.  Diagonal
+// or no preconditioning (M^T = M).  Same control flow and outputs as cg_solve.
+template <typename T>
+__device__ void bicg_true_solve(Grid& g, const Mat<T>& m, const Mat<T>& mT, Vecs<T>& v,
+                                const SolveCfg& cfg, SolveOut& out) {
+    double tol = cfg.tol, err = 0.0, dummy = 0.0;
+    if (!prologue(g, m, v, cfg, out, tol, err, dummy, false)) return;
+    const bool diag = cfg.prec == 1;
+    T* z2 = v.u1;
+    T* q2 = v.v2;
+    // shadow r2 = r; z = M^-1 r, z2 = M^-1 r2; rho = (z, r2)
+    T a0[1] = {T(0)};
+    TF_FOR4(g, m, i) {
+        const V4<T> r = ld4(v.r + i);
+        V4<T> z = r;
+        if (diag) {
+            const V4<T> d = ld4(v.D + i);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) z.a[u] = jacobi(r.a[u], d.a[u]);
+        }
+        st4(v.r2 + i, r);
+        st4(v.z + i, z);
+        st4(z2 + i, z);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u < m.n) a0[0] += z.a[u] * r.a[u];
+    }
+    publish_t<1>(g, SLOT_A, a0);
+    if (!grid_sync(g, 60)) { out.exit_kind = EXIT_ABORT; return; }
+    double t0[1];
+    totals<1>(g, SLOT_A, t0);
+    double rho = t0[0], rhoold = 0.0;
+    int iter = 1;
+    for (; iter <= cfg.maxiter; ++iter) {
+        const T beta = T(iter == 1 ? 0.0 : rho / rhoold);
+        TF_FOR4(g, m, i) {
+            const V4<T> z = ld4(v.z + i), zz = ld4(z2 + i);
+            V4<T> p = z, pp = zz;
+            if (iter > 1) {
+                p = ld4(v.p + i);
+                pp = ld4(v.p2 + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    p.a[u] = z.a[u] + beta * p.a[u];
+                    pp.a[u] = zz.a[u] + beta * pp.a[u];
+                }
+            }
+            st4(v.p + i, p);
+            st4(v.p2 + i, pp);
+        }
+        if (!grid_sync(g, 61)) { out.exit_kind = EXIT_ABORT; return; }
+        T a1[1] = {T(0)};
+        for (int s = g.wg; s < m.nslices; s += g.nw) {
+            const int i = s * kWarp + g.lane;
+            const T qi = sell_row(m, s, g.lane, v.p);
+            const T q2i = sell_row(mT, s, g.lane, v.p2);
+            if (i < m.n) {
+                v.q[i] = qi;
+                q2[i] = q2i;
+                a1[0] += v.p2[i] * qi;
+            }
+        }
+        publish_t<1>(g, SLOT_B, a1);
+        if (!grid_sync(g, 62)) { out.exit_kind = EXIT_ABORT; return; }
+        double t1[1];
+        totals<1>(g, SLOT_B, t1);
+        const T alfa = T(rho / t1[0]);
+        T a3[2] = {T(0), T(0)};
+        TF_FOR4(g, m, i) {
+            V4<T> x = ld4(v.x + i), r = ld4(v.r + i), rr = ld4(v.r2 + i);
+            const V4<T> p = ld4(v.p + i), q = ld4(v.q + i), qq = ld4(q2 + i);
+            V4<T> z, zz, d;
+            if (diag) d = ld4(v.D + i);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                x.a[u] = x.a[u] + alfa * p.a[u];
+                r.a[u] = r.a[u] - alfa * q.a[u];
+                rr.a[u] = rr.a[u] - alfa * qq.a[u];
+                z.a[u] = diag ? jacobi(r.a[u], d.a[u]) : r.a[u];
+                zz.a[u] = diag ? jacobi(rr.a[u], d.a[u]) : rr.a[u];
+                if (i + u < m.n) {
+                    a3[0] += r.a[u] * r.a[u];
+                    a3[1] += z.a[u] * rr.a[u];
+                }
+            }
+            st4(v.x + i, x);
+            st4(v.r + i, r);
+            st4(v.r2 + i, rr);
+            st4(v.z + i, z);
+            st4(z2 + i, zz);
+        }
+        publish_t<2>(g, SLOT_C, a3);
+        if (!grid_sync(g, 63)) { out.exit_kind = EXIT_ABORT; return; }
+        double t3[2];
+        totals<2>(g, SLOT_C, t3);
+        err = sqrt(t3[0]);
+        out.fin_res = err;
+        if (err < tol) {
+            out.exit_kind = EXIT_CONVERGED;
+            out.iterations = iter;
+            return;
+        }
+        if (!finite_val(err)) {
+            out.exit_kind = EXIT_NONFINITE;
+            out.iterations = cfg.maxiter + 1;
+            return;
+        }
+        rhoold = rho;
+        rho = t3[1];
+    }
+    out.exit_kind = EXIT_MAXITER;
+    out.iterations = iter;
+}
+
 // ---- mixed precision: FP32 inner Krylov inside FP64 iterative refinement ---------
 // Outer loop in FP64: r = b - A x with the FP64 values (exact row order),
 // ||r|| and the convergence test; inner solve of A d = r in FP32 (FP32 SELL

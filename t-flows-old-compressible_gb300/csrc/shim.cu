@@ -230,7 +230,8 @@ cudaError_t build_levels(DeviceTopology& t) {
     return cudaSuccess;
 }
 
-// Transposed-entry positions: for each stored (i,j), where (j,i) is stored.
+// Transposed-entry positions: for each stored (i,j), where (j,i) is stored
+// (-1 where it is not: a structurally unsymmetric pattern).
 cudaError_t build_transpose(DeviceTopology& t) {
     if (t.tpos) return cudaSuccess;
     std::vector<int> tp((size_t)t.nnz, -1);
@@ -242,6 +243,7 @@ cudaError_t build_transpose(DeviceTopology& t) {
             for (const int* p = b; p != e; ++p)
                 if (*p == i) { tp[j] = (int)(p - t.h_col.data()); break; }
         }
+    t.tsym = std::find(tp.begin(), tp.end(), -1) == tp.end();
     return upload(&t.tpos, tp.data(), tp.size());
 }
 
@@ -398,7 +400,15 @@ void record(const SolveReport& rep, tflows_result* res) {
 int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, const double* d_b,
              double* d_x, double* d_r_out, cudaStream_t s, SolveReport& rep) {
     SolveRequest rq = rq0;
-    if (rq.method == TFLOWS_METHOD_BICG_TRUE) return fail(TFLOWS_UNSUPPORTED, "true BiCG not built");
+    if (rq.method == TFLOWS_METHOD_BICG_TRUE) {
+        if (rq.precision != TFLOWS_FP64)
+            return fail(TFLOWS_UNSUPPORTED, "true BiCG runs in FP64 only");
+        if (rq.prec == 2) return fail(TFLOWS_UNSUPPORTED, "true BiCG takes prec 0 or 1");
+        if (cudaError_t e = build_transpose(tp->t); e != cudaSuccess)
+            return cuda_fail(e, "transpose map");
+        if (!tp->t.tsym)
+            return fail(TFLOWS_BAD_INPUT, "true BiCG needs a structurally symmetric pattern");
+    }
     if (rq.prec == 2) {
         if (!tp->t.ic_ok)
             return fail(TFLOWS_BAD_INPUT,
@@ -411,6 +421,9 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
     if (e != cudaSuccess) return cuda_fail(e, "workspace");
     if ((e = permute_values(tp->t, tp->ws, d_val, true, rq.precision != TFLOWS_FP64, s)) != cudaSuccess)
         return cuda_fail(e, "value layout");
+    if (rq.method == TFLOWS_METHOD_BICG_TRUE &&
+        (e = permute_transposed(tp->t, tp->ws, d_val, s)) != cudaSuccess)
+        return cuda_fail(e, "transposed values");
     // The kernels work on padded, 16-byte aligned workspace vectors: x and b
     // are staged into workspace slots 11 and 12 unless they already are them.
     const size_t nb = sizeof(double) * tp->t.n;

@@ -209,3 +209,23 @@ def test_full_size_config2_properties():
         true_r = s.b - s.scipy() @ x[s.NB + 1:]
         assert np.linalg.norm(true_r) < 2 * s.tol
         assert abs(np.linalg.norm(r) - out.FinRes) <= 1e-10 * out.IniRes
+
+
+def test_true_bicg_extension_converges_where_cg_recurrence_fails():
+    """BICG_TRUE (shadow sequence multiplied by A^T) on a strongly
+    nonsymmetric system: reaches the tolerance and the direct solution;
+    not a reference method, so it is checked against scipy."""
+    import scipy.sparse.linalg as spla
+    s = mesh.convection_diffusion_system(14, 12, 10, perturb=0.2, seed=5, dt=1.0)
+    tol = 1e-10 * float(np.linalg.norm(s.b))
+    for prec in (0, 1):
+        x, r = s.x.copy(), s.b.copy()
+        out = tflows.solve_ex("bicg_true", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
+                              x, r, prec, 2000, tol)
+        assert out.status == tflows.OK, out
+        xd = spla.spsolve(s.scipy().tocsc(), s.b)
+        assert rel_diff(x[s.NB + 1:], xd) < 1e-7
+        assert np.linalg.norm(s.b - s.scipy() @ x[s.NB + 1:]) < 2 * tol
+    with pytest.raises(tflows.SolverError):
+        tflows.solve_ex("bicg_true", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
+                        s.x.copy(), s.b.copy(), 2, 100, tol)
