@@ -171,6 +171,25 @@ int tflows_solve_batched_device(int count, tflows_topology *const *topos,
                                 const int *maxiters, const double *tols,
                                 void *stream, tflows_result *results);
 
+/* Graph-captured batched solve.  tflows_plan_create records, for fixed
+ * device pointers, everything a batched solve does -- value layout, staging
+ * of x and b, the one persistent cooperative launch, result records and the
+ * copy of x back -- into a CUDA graph with its own workspaces;
+ * tflows_plan_launch replays it on `stream` (asynchronous; the caller may
+ * change the contents of vals/bs/xs between replays, e.g. once per time
+ * step); tflows_plan_results waits for the last replay and fills one result
+ * per system. */
+typedef struct tflows_plan tflows_plan;
+int tflows_plan_create(tflows_plan **out, int count,
+                       tflows_topology *const *topos, const int *methods,
+                       const int *precs, const tflows_options *opt,
+                       const double *const *vals, const double *const *bs,
+                       double *const *xs, const int *maxiters,
+                       const double *tols);
+int tflows_plan_launch(tflows_plan *plan, void *stream);
+int tflows_plan_results(tflows_plan *plan, tflows_result *results);
+void tflows_plan_destroy(tflows_plan *plan);
+
 /* grad_val[k] = -lambda[row(k)] * x[col(k)] over the stored pattern: the
  * gradient of a scalar loss with respect to the matrix entries, given the
  * adjoint solution lambda (A^T lambda = dL/dx) and the solution x. */

@@ -135,6 +135,11 @@ SIGNATURES = {
     "tflows_pattern_outer": ([_VP, _VP, _VP, _VP, _VP], ctypes.c_int),
     "tflows_spmv_device": ([_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP,
                             ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "tflows_plan_create": ([ctypes.POINTER(_VP), ctypes.c_int, _VP, _VP, _VP,
+                            ctypes.POINTER(Options), _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "tflows_plan_launch": ([_VP, _VP], ctypes.c_int),
+    "tflows_plan_results": ([_VP, ctypes.POINTER(Result)], ctypes.c_int),
+    "tflows_plan_destroy": ([_VP], None),
     "tflows_cg_noalloc": ([ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
                            ctypes.c_int, ctypes.c_double, _VP, _I, _D, _D], ctypes.c_int),
 }

@@ -309,3 +309,49 @@ def solve_batched(topos, vals, bs, xs, methods, precs, maxiters, tols, opts=None
     if raise_on_error and st in (BAD_INPUT, CUDA_ERROR, NO_DEVICE, UNSUPPORTED, TIMEOUT):
         raise SolverError(st, last_error())
     return [r.as_dict() for r in res]
+
+
+class Plan:
+    """A batched solve recorded once into a CUDA graph (tflows_plan_*).
+
+    The tensors passed here are bound by address: change their contents
+    (new matrix values, right-hand sides, initial guesses) and call
+    ``launch()`` again; ``results()`` waits and returns one record per
+    system."""
+
+    def __init__(self, topos, vals, bs, xs, methods, precs, maxiters, tols, opts=None):
+        n = len(topos)
+        VP = ctypes.c_void_p * n
+        self._keep = (topos, vals, bs, xs)
+        self._n = n
+        self._h = ctypes.c_void_p()
+        st = lib().tflows_plan_create(
+            ctypes.byref(self._h), n, VP(*[t.handle.value for t in topos]),
+            (ctypes.c_int * n)(*[int(METHODS.get(m, m)) for m in methods]),
+            (ctypes.c_int * n)(*[int(p) for p in precs]), ctypes.byref(opts) if opts else None,
+            VP(*[v.data_ptr() for v in vals]), VP(*[v.data_ptr() for v in bs]),
+            VP(*[v.data_ptr() for v in xs]), (ctypes.c_int * n)(*[int(m) for m in maxiters]),
+            (ctypes.c_double * n)(*[float(t) for t in tols]))
+        if st != OK:
+            raise SolverError(st, last_error())
+
+    def launch(self):
+        st = lib().tflows_plan_launch(self._h, _stream())
+        if st != OK:
+            raise SolverError(st, last_error())
+
+    def results(self):
+        res = (_native.Result * self._n)()
+        lib().tflows_plan_results(self._h, res)
+        return [r.as_dict() for r in res]
+
+    def close(self):
+        if self._h:
+            lib().tflows_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

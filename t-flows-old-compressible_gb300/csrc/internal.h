@@ -122,6 +122,15 @@ int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, doubl
 // r <- r - A x (Resid), device arrays.
 // All systems in one cooperative launch (block groups sized by expected work).
 int run_batch(std::vector<BatchSpec>& specs, cudaStream_t s, double* seconds);
+// The same split into a capturable enqueue (parameters, launch, result
+// records into pinned memory) and a collect step (synchronise, reports).
+struct BatchLaunch;
+BatchLaunch* batch_create();
+void batch_destroy(BatchLaunch* L);
+// Allocate the launch buffers for `count` systems up front (before a capture).
+cudaError_t batch_reserve(BatchLaunch* L, int count);
+int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s);
+int batch_collect(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s, double seconds);
 cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, double* r,
                       cudaStream_t s);
 cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, double* y, bool fp32,

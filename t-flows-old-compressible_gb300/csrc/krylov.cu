@@ -618,25 +618,90 @@ int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, do
     return launch_and_report(kern, P, t, ws, rq, s, rep, e);
 }
 
-int run_batch(std::vector<BatchSpec>& specs, cudaStream_t s, double* seconds) {
+// Persistent launch state of a batched solve: pinned host and device copies
+// of the per-system parameters and the block -> system map, and pinned room
+// for the per-system result records.  Every stream operation it issues is
+// capturable, so a batch can be recorded once into a CUDA graph and replayed.
+struct BatchLaunch {
+    BatchItem* h_items = nullptr;
+    BatchItem* d_items = nullptr;
+    int* h_map = nullptr;
+    int* d_map = nullptr;
+    DevState* h_state = nullptr;
+    int item_cap = 0;
+    int map_cap = 0;
+    int total = 0;
+};
+
+BatchLaunch* batch_create() { return new BatchLaunch(); }
+
+void batch_destroy(BatchLaunch* L) {
+    if (!L) return;
+    if (L->h_items) cudaFreeHost(L->h_items);
+    if (L->h_map) cudaFreeHost(L->h_map);
+    if (L->h_state) cudaFreeHost(L->h_state);
+    if (L->d_items) cudaFree(L->d_items);
+    if (L->d_map) cudaFree(L->d_map);
+    delete L;
+}
+
+namespace {
+
+cudaError_t grow(BatchLaunch& L, int count, int total) {
+    cudaError_t e = cudaSuccess;
+    if (count > L.item_cap) {
+        if (L.h_items) cudaFreeHost(L.h_items);
+        if (L.d_items) cudaFree(L.d_items);
+        if (L.h_state) cudaFreeHost(L.h_state);
+        L.h_items = nullptr;
+        L.d_items = nullptr;
+        L.h_state = nullptr;
+        if ((e = cudaMallocHost(&L.h_items, sizeof(BatchItem) * count)) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&L.d_items, sizeof(BatchItem) * count)) != cudaSuccess) return e;
+        if ((e = cudaMallocHost(&L.h_state, sizeof(DevState) * count)) != cudaSuccess) return e;
+        L.item_cap = count;
+    }
+    if (total > L.map_cap) {
+        if (L.h_map) cudaFreeHost(L.h_map);
+        if (L.d_map) cudaFree(L.d_map);
+        L.h_map = nullptr;
+        L.d_map = nullptr;
+        if ((e = cudaMallocHost(&L.h_map, sizeof(int) * total)) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&L.d_map, sizeof(int) * total)) != cudaSuccess) return e;
+        L.map_cap = total;
+    }
+    return e;
+}
+
+void fail_all(std::vector<BatchSpec>& specs, int status, const std::string& msg) {
+    for (auto& sp : specs) {
+        sp.rep->status = status;
+        sp.rep->message = msg;
+    }
+}
+
+}  // namespace
+
+cudaError_t batch_reserve(BatchLaunch* L, int count) {
+    const int maxb = std::max(max_coresident(batch_kernel<0>, kBlock),
+                              max_coresident(batch_kernel<1>, kBlock));
+    return grow(*L, count, maxb);
+}
+
+int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s) {
     const int count = (int)specs.size();
     if (count == 0) return ST_OK;
     const bool mixed = specs[0].rq.precision == 1;
     for (auto& sp : specs)
         if ((sp.rq.precision == 1) != mixed) {
-            for (auto& q : specs) {
-                q.rep->status = ST_BAD_INPUT;
-                q.rep->message = "one precision per batched launch";
-            }
+            fail_all(specs, ST_BAD_INPUT, "one precision per batched launch");
             return ST_BAD_INPUT;
         }
     auto kern = mixed ? batch_kernel<1> : batch_kernel<0>;
     const int maxb = max_coresident(kern, kBlock);
     if (count > maxb) {
-        for (auto& sp : specs) {
-            sp.rep->status = ST_BAD_INPUT;
-            sp.rep->message = "more systems than co-resident blocks (" + std::to_string(maxb) + ")";
-        }
+        fail_all(specs, ST_BAD_INPUT,
+                 "more systems than co-resident blocks (" + std::to_string(maxb) + ")");
         return ST_BAD_INPUT;
     }
     // Blocks per system in proportion to the expected work, N^(4/3) (rows
@@ -651,7 +716,8 @@ int run_batch(std::vector<BatchSpec>& specs, cudaStream_t s, double* seconds) {
     std::vector<int> nb(count);
     int total = 0;
     for (int k = 0; k < count; ++k) {
-        const int cap = std::max(1, blocks_for(specs[k].t->nslices));
+        const int cap = specs[k].rq.grid > 0 ? specs[k].rq.grid
+                                             : std::max(1, blocks_for(specs[k].t->nslices));
         nb[k] = std::max(1, std::min(cap, (int)std::floor((maxb - count) * w[k] / wsum) + 1));
         total += nb[k];
     }
@@ -660,61 +726,88 @@ int run_batch(std::vector<BatchSpec>& specs, cudaStream_t s, double* seconds) {
         --nb[big];
         --total;
     }
-    std::vector<BatchItem> items(count);
-    std::vector<int> block_item(total);
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = grow(*L, count, total);
+    if (e != cudaSuccess) {
+        fail_all(specs, ST_CUDA_ERROR, std::string("batch buffers: ") + cudaGetErrorString(e));
+        return ST_CUDA_ERROR;
+    }
     int b0 = 0;
     for (int k = 0; k < count; ++k) {
         BatchSpec& sp = specs[k];
-        BatchItem& it = items[k];
+        BatchItem& it = L->h_items[k];
         std::memset(&it, 0, sizeof(it));
         it.b0 = b0;
         it.nb = nb[k];
         it.method = sp.rq.method == 2 ? 2 : 0;
-        it.mixed = sp.rq.precision == 1;
-        cudaError_t ek = it.mixed ? prepare_mixed(*sp.t, *sp.ws, sp.rq, sp.x, sp.r, s, it.PM)
-                                  : prepare_fp64(*sp.t, *sp.ws, sp.rq, sp.x, sp.r, s, it.P64);
+        it.mixed = mixed;
+        cudaError_t ek = mixed ? prepare_mixed(*sp.t, *sp.ws, sp.rq, sp.x, sp.r, s, it.PM)
+                               : prepare_fp64(*sp.t, *sp.ws, sp.rq, sp.x, sp.r, s, it.P64);
         if (ek != cudaSuccess) e = ek;
-        for (int j = 0; j < nb[k]; ++j) block_item[b0 + j] = k;
+        for (int j = 0; j < nb[k]; ++j) L->h_map[b0 + j] = k;
         b0 += nb[k];
     }
-    BatchItem* d_items = nullptr;
-    int* d_map = nullptr;
-    if (e == cudaSuccess) e = cudaMallocAsync(&d_items, sizeof(BatchItem) * count, s);
-    if (e == cudaSuccess) e = cudaMallocAsync(&d_map, sizeof(int) * total, s);
+    L->total = total;
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_items, items.data(), sizeof(BatchItem) * count, cudaMemcpyHostToDevice, s);
+        e = cudaMemcpyAsync(L->d_items, L->h_items, sizeof(BatchItem) * count,
+                            cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_map, block_item.data(), sizeof(int) * total, cudaMemcpyHostToDevice, s);
-    cudaEvent_t e0 = specs[0].ws->ev0, e1 = specs[0].ws->ev1;
-    cudaEventRecord(e0, s);
+        e = cudaMemcpyAsync(L->d_map, L->h_map, sizeof(int) * total, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
-        void* args[] = {&d_items, &d_map};
-        e = cudaLaunchCooperativeKernel((const void*)kern, dim3(total), dim3(kBlock), args, 0, s);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(total);
+        cfg.blockDim = dim3(kBlock);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const BatchItem* di = L->d_items;
+        const int* dm = L->d_map;
+        e = cudaLaunchKernelEx(&cfg, kern, di, dm);
     }
-    cudaEventRecord(e1, s);
-    std::vector<DevState> st(count);
     for (int k = 0; k < count && e == cudaSuccess; ++k)
-        e = cudaMemcpyAsync(&st[k], specs[k].ws->state, sizeof(DevState), cudaMemcpyDeviceToHost, s);
-    if (d_items) cudaFreeAsync(d_items, s);
-    if (d_map) cudaFreeAsync(d_map, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        e = cudaMemcpyAsync(L->h_state + k, specs[k].ws->state, sizeof(DevState),
+                            cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) {
-        for (auto& sp : specs) {
-            sp.rep->status = ST_CUDA_ERROR;
-            sp.rep->message = std::string("batched solver: ") + cudaGetErrorString(e);
-        }
+        fail_all(specs, ST_CUDA_ERROR, std::string("batched solver: ") + cudaGetErrorString(e));
         return ST_CUDA_ERROR;
     }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (seconds) *seconds = ms * 1e-3;
+    return ST_OK;
+}
+
+int batch_collect(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s, double seconds) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        fail_all(specs, ST_CUDA_ERROR, std::string("batched solver: ") + cudaGetErrorString(e));
+        return ST_CUDA_ERROR;
+    }
     int worst = ST_OK;
-    for (int k = 0; k < count; ++k) {
-        fill_report(*specs[k].t, specs[k].rq, st[k], ms * 1e-3, *specs[k].rep);
-        worst = std::max(worst, st[k].status);
+    for (int k = 0; k < (int)specs.size(); ++k) {
+        fill_report(*specs[k].t, specs[k].rq, L->h_state[k], seconds, *specs[k].rep);
+        worst = std::max(worst, L->h_state[k].status);
     }
     return worst;
+}
+
+int run_batch(std::vector<BatchSpec>& specs, cudaStream_t s, double* seconds) {
+    if (specs.empty()) return ST_OK;
+    BatchLaunch* L = batch_create();
+    cudaEvent_t e0 = specs[0].ws->ev0, e1 = specs[0].ws->ev1;
+    cudaEventRecord(e0, s);
+    int st = batch_enqueue(L, specs, s);
+    cudaEventRecord(e1, s);
+    if (st == ST_OK) {
+        cudaStreamSynchronize(s);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (seconds) *seconds = ms * 1e-3;
+        st = batch_collect(L, specs, s, ms * 1e-3);
+    } else {
+        cudaStreamSynchronize(s);
+    }
+    batch_destroy(L);
+    return st;
 }
 
 cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, double* r,

@@ -825,6 +825,125 @@ int tflows_solve_batched_device(int count, tflows_topology* const* topos, const 
     return worst;
 }
 
+struct tflows_plan {
+    std::vector<tflows_topology*> topos;
+    std::vector<std::unique_ptr<Workspace>> ws;
+    std::vector<SolveReport> reps;
+    std::vector<BatchSpec> specs;
+    BatchLaunch* launch = nullptr;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t last = nullptr;
+    int device = 0;
+};
+
+int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* topos,
+                       const int* methods, const int* precs, const tflows_options* opt,
+                       const double* const* vals, const double* const* bs, double* const* xs,
+                       const int* maxiters, const double* tols) {
+    t_error.clear();
+    if (!out || count <= 0 || !topos || !methods || !precs || !vals || !bs || !xs || !maxiters ||
+        !tols)
+        return fail(TFLOWS_BAD_INPUT, "null argument");
+    tflows_options o;
+    if (opt) o = *opt;
+    else default_opts(&o);
+    auto plan = std::make_unique<tflows_plan>();
+    plan->device = topos[0]->t.device;
+    cudaSetDevice(plan->device);
+    plan->reps.resize(count);
+    plan->specs.resize(count);
+    for (int k = 0; k < count; ++k) {
+        tflows_topology* tp = topos[k];
+        if (!tp || !vals[k] || !bs[k] || !xs[k]) return fail(TFLOWS_BAD_INPUT, "null system");
+        if (tp->t.device != plan->device) return fail(TFLOWS_BAD_INPUT, "systems on different devices");
+        std::lock_guard<std::mutex> lk(tp->mu);
+        SolveRequest rq = make_request(o, methods[k], precs[k], maxiters[k], tols[k]);
+        if (rq.method == TFLOWS_METHOD_BICG_TRUE)
+            return fail(TFLOWS_UNSUPPORTED, "true BiCG is not available in batched solves");
+        if (rq.prec == 2) {
+            if (!tp->t.ic_ok) return fail(TFLOWS_BAD_INPUT, "IC(0) needs a triangular-ordered pattern");
+            if (cudaError_t e = build_levels(tp->t); e != cudaSuccess) return cuda_fail(e, "level sets");
+        }
+        plan->ws.emplace_back(new Workspace());
+        if (cudaError_t e = ensure_workspace(*plan->ws.back(), tp->t); e != cudaSuccess)
+            return cuda_fail(e, "workspace");
+        Workspace* ws = plan->ws.back().get();
+        plan->specs[k] = BatchSpec{&tp->t, ws, rq, ws->vec64 + 11 * ws->vec_cap,
+                                   ws->vec64 + 12 * ws->vec_cap, &plan->reps[k]};
+        plan->topos.push_back(tp);
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&plan->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "plan stream");
+    plan->launch = batch_create();
+    if ((e = batch_reserve(plan->launch, count)) != cudaSuccess) {
+        tflows_plan_destroy(plan.release());
+        return cuda_fail(e, "plan buffers");
+    }
+    cudaStream_t s = plan->cap;
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+    int st = TFLOWS_OK;
+    for (int k = 0; k < count && e == cudaSuccess; ++k) {
+        BatchSpec& sp = plan->specs[k];
+        const size_t nb = sizeof(double) * sp.t->n;
+        e = permute_values(*sp.t, *sp.ws, vals[k], true, sp.rq.precision != TFLOWS_FP64, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(sp.x, xs[k], nb, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(sp.r, bs[k], nb, cudaMemcpyDeviceToDevice, s);
+    }
+    if (e == cudaSuccess) st = batch_enqueue(plan->launch, plan->specs, s);
+    for (int k = 0; k < count && e == cudaSuccess && st == TFLOWS_OK; ++k)
+        e = cudaMemcpyAsync(xs[k], plan->specs[k].x, sizeof(double) * plan->specs[k].t->n,
+                            cudaMemcpyDeviceToDevice, s);
+    cudaError_t ee = cudaStreamEndCapture(s, &plan->graph);
+    if (e == cudaSuccess) e = ee;
+    if (st != TFLOWS_OK) {
+        std::string msg = plan->reps[0].message;
+        tflows_plan_destroy(plan.release());
+        return fail(st, msg);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
+    if (e != cudaSuccess) {
+        tflows_plan_destroy(plan.release());
+        return fail(TFLOWS_UNSUPPORTED, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
+    *out = plan.release();
+    t_status = TFLOWS_OK;
+    return TFLOWS_OK;
+}
+
+int tflows_plan_launch(tflows_plan* plan, void* stream) {
+    if (!plan || !plan->exec) return fail(TFLOWS_BAD_INPUT, "null plan");
+    cudaSetDevice(plan->device);
+    cudaError_t e = cudaGraphLaunch(plan->exec, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+    plan->last = (cudaStream_t)stream;
+    t_status = TFLOWS_OK;
+    return TFLOWS_OK;
+}
+
+int tflows_plan_results(tflows_plan* plan, tflows_result* results) {
+    if (!plan) return fail(TFLOWS_BAD_INPUT, "null plan");
+    cudaSetDevice(plan->device);
+    int worst = batch_collect(plan->launch, plan->specs, plan->last, 0.0);
+    for (size_t k = 0; k < plan->reps.size(); ++k) record(plan->reps[k], results ? results + k : nullptr);
+    t_status = worst;
+    return worst;
+}
+
+void tflows_plan_destroy(tflows_plan* plan) {
+    if (!plan) return;
+    cudaSetDevice(plan->device);
+    if (plan->last) cudaStreamSynchronize(plan->last);
+    if (plan->exec) cudaGraphExecDestroy(plan->exec);
+    if (plan->graph) cudaGraphDestroy(plan->graph);
+    if (plan->cap) cudaStreamDestroy(plan->cap);
+    if (plan->launch) batch_destroy(plan->launch);
+    for (auto& w : plan->ws) free_workspace(*w);
+    delete plan;
+}
+
 int tflows_pattern_outer(tflows_topology* topo, const double* lambda, const double* x,
                          double* grad_val, void* stream) {
     if (!topo || !lambda || !x || !grad_val) return fail(TFLOWS_BAD_INPUT, "null argument");

@@ -72,3 +72,33 @@ def test_batched_repeated_pattern():
     for k in range(5):
         assert res[k]["status"] == tflows.OK
         assert np.linalg.norm(rhs[k] - A @ xs[k].cpu().numpy()) < 2 * tols[k]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_plan_replays_with_new_data(precision):
+    """One CUDA graph holds the whole batched solve; each replay picks up new
+    right-hand sides written in place (as a time loop would) and must reach
+    the tolerance relative to them."""
+    import torch
+    systems = _systems()
+    opts = tflows.options(precision=precision, tol_mode=tflows.TOL_RELATIVE)
+    topos = [tflows.Topology.from_system(s) for s, _, _ in systems]
+    vals = [_dev(s.A[:-1]) for s, _, _ in systems]
+    bs = [torch.zeros(s.N, dtype=torch.float64, device="cuda") for s, _, _ in systems]
+    xs = [torch.zeros(s.N, dtype=torch.float64, device="cuda") for s, _, _ in systems]
+    plan = tflows.Plan(topos, vals, bs, xs, [m for _, m, _ in systems],
+                       [p for _, _, p in systems], [3000] * len(systems), [1e-10] * len(systems),
+                       opts)
+    rng = np.random.default_rng(1)
+    for step in range(3):
+        rhs = [s.b * (1.0 + step) + rng.uniform(-1, 1, s.N) for s, _, _ in systems]
+        for k in range(len(systems)):
+            bs[k].copy_(_dev(rhs[k]))
+            xs[k].zero_()
+        plan.launch()
+        res = plan.results()
+        for k, (s, m, p) in enumerate(systems):
+            assert res[k]["status"] == tflows.OK, (step, k, res[k])
+            x = xs[k].cpu().numpy()
+            assert np.linalg.norm(rhs[k] - s.scipy() @ x) < 2e-10 * np.linalg.norm(rhs[k]), (step, k)
+    plan.close()
