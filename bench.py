@@ -48,6 +48,16 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+def profiled_traffic(kernel, workload, method, prec):
+    """DRAM bytes per launch of this kernel on this workload from the committed
+    ncu summary (profiles/traffic.json), or None when it was not captured."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(f"{kernel}|{workload}|{method}|{prec}")
+    except Exception:
+        return None
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
         os.environ.get("LOCAL_RANK", "0"))
@@ -238,6 +248,54 @@ def mixed_vs_fp64(pkg, dev, scale, prec, reps):
             "mixed_rel_diff_vs_fp64": d}
 
 
+def batched_cfg4(pkg, dev, reps, count=48):
+    """48 independent systems of uneven size (log-uniform 16^3..160^3 cells),
+    odd ones variable-density pressure (CG + IC), even ones scalar transport
+    (BiCG + diagonal), mixed precision with FP64 refinement to 1e-8 relative,
+    solved by one graph-captured persistent launch per replay."""
+    import torch
+    shapes = pkg.mesh.batch_sizes(count)
+    systems = []
+    for k, (nx, ny, nz) in enumerate(shapes):
+        if k % 2:
+            systems.append((pkg.mesh.pressure_system(nx, ny, nz, perturb=0.2, seed=100 + k,
+                                                     variable_density=True), "cg", 2))
+        else:
+            systems.append((pkg.mesh.convection_diffusion_system(nx, ny, nz, perturb=0.2,
+                                                                 seed=100 + k), "bicg", 1))
+    topos = [pkg.Topology.from_system(s) for s, _, _ in systems]
+    vals = [torch.from_numpy(s.A[:-1].copy()).to(dev) for s, _, _ in systems]
+    bs = [torch.from_numpy(s.b.copy()).to(dev) for s, _, _ in systems]
+    xs = [torch.zeros(s.N, dtype=torch.float64, device=dev) for s, _, _ in systems]
+    opts = pkg.options(precision=pkg.MIXED, tol_mode=pkg.TOL_RELATIVE)
+    plan = pkg.Plan(topos, vals, bs, xs, [m for _, m, _ in systems], [p for _, _, p in systems],
+                    [20000] * count, [1e-8] * count, opts)
+    plan.launch()
+    res = plan.results()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        for x in xs:
+            x.zero_()
+        plan.launch()
+    e1.record()
+    res = plan.results()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    rows = sum(s.N for s, _, _ in systems)
+    byts = sum(r["bytes"] for r in res)
+    ok = sum(1 for r in res if r["status"] == pkg.OK)
+    plan.close()
+    return {"workload": f"{count} systems, sizes {min(s.N for s, _, _ in systems)}.."
+                        f"{max(s.N for s, _, _ in systems)} rows (total {rows}), odd: CG+IC "
+                        "pressure, even: BiCG+diag transport, mixed precision, tol 1e-8 relative, "
+                        "one graph-captured cooperative launch",
+            "ms_per_batch": ms, "systems_per_s": count * 1e3 / ms, "converged": ok,
+            "max_iterations": max(r["iterations"] for r in res),
+            "gbs": byts / (ms * 1e-3) / 1e9}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -254,6 +312,9 @@ def main():
     ap.add_argument("--compare-scale", type=int, default=256,
                     help="edge of the cfg3 mixed-vs-FP64 comparison (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched (cfg4) block")
+    ap.add_argument("--ic-compare-scale", type=int, default=128,
+                    help="edge of the IC mixed-vs-FP64 comparison (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -311,8 +372,10 @@ def main():
         "time_to_tol_ms": 1e3 * el / args.steps,
     }
     achieved = kern_b / kern_s / 1e9
+    kname = "mixed_kernel" if args.precision == "mixed" else "krylov_kernel_fp64"
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": None,
+                        "frac": achieved / peak,
+                        "traffic": profiled_traffic(kname, s.name, method, prec),
                         "kernel": ("mixed_kernel" if args.precision == "mixed" else
                                    "krylov_kernel<double>") + " (one persistent launch per solve)",
                         "peak_kind": peak_kind}
@@ -362,6 +425,13 @@ def main():
 
     if rank == 0 and args.compare_scale:
         line["mixed_vs_fp64"] = mixed_vs_fp64(pkg, dev, args.compare_scale, 1, 1)
+        torch.cuda.empty_cache()
+    if rank == 0 and args.ic_compare_scale:
+        line["mixed_vs_fp64_ic"] = mixed_vs_fp64(pkg, dev, args.ic_compare_scale, 2, 1)
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.no_batch:
+        line["batched_cfg4"] = batched_cfg4(pkg, dev, 2)
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_cpu_baseline:
         v, n, it, el_c = cpu_reference_throughput(s, method, prec, 1, args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",

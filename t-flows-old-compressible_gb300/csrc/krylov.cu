@@ -69,6 +69,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) krylov_kernel(KParams<T> P
         s->status = status_of(out, P.ctl);
         s->exit_kind = out.exit_kind;
         s->iterations = out.iterations;
+        s->inner_iters = 0;
+        s->refinements = 0;
         s->ini_res = out.ini_res;
         s->fin_res = out.fin_res;
         s->bnrm2 = out.bnrm2;
@@ -565,6 +567,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks)
             s->status = status_of(out, P.ctl);
             s->exit_kind = out.exit_kind;
             s->iterations = out.iterations;
+            s->inner_iters = 0;
+            s->refinements = 0;
             s->ini_res = out.ini_res;
             s->fin_res = out.fin_res;
             s->bnrm2 = out.bnrm2;
