@@ -219,36 +219,55 @@ def device_solves(pkg, topo, val, b, x, method, prec, tol, opts, steps, warmup, 
     return e0.elapsed_time(e1) * 1e-3, out
 
 
-def mixed_vs_fp64(pkg, dev, scale, prec, reps):
-    """The variable-density pressure system (cfg3): CG with the given
+IC_VARIANTS = (("exact_fp32", {}), ("exact_bf16", {"ic_bf16": 1}),
+               ("jacobi1_bf16", {"ic_sweeps": 1, "ic_bf16": 1}),
+               ("jacobi2_bf16", {"ic_sweeps": 2, "ic_bf16": 1}),
+               ("jacobi2_fp32", {"ic_sweeps": 2}),
+               ("jacobi4_bf16", {"ic_sweeps": 4, "ic_bf16": 1}))
+
+
+def mixed_vs_fp64(pkg, dev, scale, precs, reps):
+    """The variable-density pressure system (cfg3): CG with each given
     preconditioner in FP64 (reference arithmetic) and in mixed precision
-    (FP32 inner solves, FP64 refinement), same absolute tolerance."""
-    import numpy as np
+    (FP32 inner solves, FP64 refinement), same absolute tolerance.  With
+    IC(0) the mixed solve is run with each factor variant (FP32 or BF16
+    factor entries, exact triangular solves or k Jacobi sweeps)."""
     import torch
     s = make_workload(pkg, "cfg3", scale)
     topo = pkg.Topology.from_system(s)
     val = torch.from_numpy(s.A[:-1].copy()).to(dev)
     b = torch.from_numpy(s.b.copy()).to(dev)
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
-    res = {}
-    xs = {}
-    for mode, opts in (("fp64", pkg.options(precision=pkg.FP64)),
-                       ("mixed", pkg.options(precision=pkg.MIXED))):
+
+    def run(prec, opts):
         el, out = device_solves(pkg, topo, val, b, x, "cg", prec, s.tol, opts, reps, 1)
         r = out[-1]
-        res[mode] = {"ms": 1e3 * el / reps, "iterations": r["iterations"],
-                     "refinements": r["refinements"], "fin_res": r["fin_res"],
-                     "gbs": r["bytes"] / r["seconds"] / 1e9, "status": r["status"]}
-        xs[mode] = x.clone()
-    d = float((xs["mixed"] - xs["fp64"]).abs().max() / xs["fp64"].abs().max())
+        return {"ms": 1e3 * el / reps, "iterations": r["iterations"],
+                "refinements": r["refinements"], "fin_res": r["fin_res"],
+                "gbs": r["bytes"] / r["seconds"] / 1e9, "status": r["status"]}, x.clone()
+
+    result = {}
+    for prec in precs:
+        fp, x64 = run(prec, pkg.options(precision=pkg.FP64))
+        variants = IC_VARIANTS if prec == 2 else (("jacobi_fp32", {}),)
+        mixed = {}
+        for label, kw in variants:
+            rec, xm = run(prec, pkg.options(precision=pkg.MIXED, **kw))
+            rec["rel_diff_vs_fp64"] = float((xm - x64).abs().max() / x64.abs().max())
+            mixed[label] = rec
+        ok = [k for k in mixed if mixed[k]["status"] == pkg.OK] or list(mixed)
+        best = min(ok, key=lambda k: mixed[k]["ms"])
+        result[prec] = {"workload": f"{s.name}, CG prec {prec}, tol 1e-8*||b|| absolute",
+                        "n": s.N, "fp64": fp, "mixed": mixed[best], "mixed_variant": best,
+                        "speedup": fp["ms"] / mixed[best]["ms"],
+                        "mixed_rel_diff_vs_fp64": mixed[best]["rel_diff_vs_fp64"]}
+        if len(mixed) > 1:
+            result[prec]["all_mixed_variants"] = mixed
     topo.close()
-    return {"workload": f"{s.name}, CG prec {prec}, tol 1e-8*||b|| absolute", "n": s.N,
-            "fp64": res["fp64"], "mixed": res["mixed"],
-            "speedup": res["fp64"]["ms"] / res["mixed"]["ms"],
-            "mixed_rel_diff_vs_fp64": d}
+    return result
 
 
-def batched_cfg4(pkg, dev, reps, count=48):
+def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
     """48 independent systems of uneven size (log-uniform 16^3..160^3 cells),
     odd ones variable-density pressure (CG + IC), even ones scalar transport
     (BiCG + diagonal), mixed precision with FP64 refinement to 1e-8 relative,
@@ -267,9 +286,10 @@ def batched_cfg4(pkg, dev, reps, count=48):
     vals = [torch.from_numpy(s.A[:-1].copy()).to(dev) for s, _, _ in systems]
     bs = [torch.from_numpy(s.b.copy()).to(dev) for s, _, _ in systems]
     xs = [torch.zeros(s.N, dtype=torch.float64, device=dev) for s, _, _ in systems]
-    opts = pkg.options(precision=pkg.MIXED, tol_mode=pkg.TOL_RELATIVE)
+    opts = pkg.options(precision=pkg.MIXED, tol_mode=pkg.TOL_RELATIVE, autotune=int(autotune))
     plan = pkg.Plan(topos, vals, bs, xs, [m for _, m, _ in systems], [p for _, _, p in systems],
                     [20000] * count, [1e-8] * count, opts)
+    tuning = plan.tuning()
     plan.launch()
     res = plan.results()
     torch.cuda.synchronize()
@@ -292,6 +312,8 @@ def batched_cfg4(pkg, dev, reps, count=48):
                         "pressure, even: BiCG+diag transport, mixed precision, tol 1e-8 relative, "
                         "one graph-captured cooperative launch",
             "ms_per_batch": ms, "systems_per_s": count * 1e3 / ms, "converged": ok,
+            "tuning": tuning,
+            "group_blocks": [r["grid_blocks"] for r in res],
             "max_iterations": max(r["iterations"] for r in res),
             "gbs": byts / (ms * 1e-3) / 1e9}
 
@@ -313,7 +335,9 @@ def main():
                     help="edge of the cfg3 mixed-vs-FP64 comparison (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (cfg4) block")
-    ap.add_argument("--ic-compare-scale", type=int, default=128,
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="fixed launch shape (256 threads, one slice per warp)")
+    ap.add_argument("--ic-compare-scale", type=int, default=256,
                     help="edge of the IC mixed-vs-FP64 comparison (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -342,7 +366,13 @@ def main():
     val = torch.from_numpy(s.A[:-1].copy()).to(dev)
     b = torch.from_numpy(s.b.copy()).to(dev)
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
-    opts = pkg.options(precision=pkg.MIXED if args.precision == "mixed" else pkg.FP64)
+    prec_mode = pkg.MIXED if args.precision == "mixed" else pkg.FP64
+    opts = pkg.options(precision=prec_mode, autotune=int(not args.no_autotune))
+    tuning = None
+    if not args.no_autotune:
+        # launch shape (threads per block, rows per warp) timed on this
+        # system before the timed region; every timed solve uses it
+        tuning = topo.autotune(val, b, method, prec, opts=pkg.options(precision=prec_mode))
 
     def barrier():
         if world > 1:
@@ -367,7 +397,10 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-        "data": "synthetic", "config": workload_config(s, method, prec, args.precision),
+        "data": "synthetic",
+        "config": dict(workload_config(s, method, prec, args.precision),
+                       launch=({"autotuned": True, **tuning} if tuning else
+                               {"autotuned": False, "block_size": 256})),
         "iterations": int(statistics.median(iters)),
         "time_to_tol_ms": 1e3 * el / args.steps,
     }
@@ -385,7 +418,7 @@ def main():
         A_h = torch.from_numpy(s.A.copy()).pin_memory().numpy()
         x_h = torch.zeros(s.NB + s.N + 1, dtype=torch.float64).pin_memory().numpy()
         r_h = torch.zeros(s.N, dtype=torch.float64).pin_memory().numpy()
-        pkg.set_options(precision=pkg.MIXED if args.precision == "mixed" else pkg.FP64)
+        pkg.set_options(precision=prec_mode, autotune=int(not args.no_autotune))
         legacy = {"cg": pkg.cg, "bicg": pkg.bicg, "cgs": pkg.cgs}[method]
         e2e_t = 0.0
         for k in range(args.warmup + args.steps):
@@ -423,14 +456,20 @@ def main():
     del val, b, x, y, xs
     torch.cuda.empty_cache()
 
-    if rank == 0 and args.compare_scale:
-        line["mixed_vs_fp64"] = mixed_vs_fp64(pkg, dev, args.compare_scale, 1, 1)
-        torch.cuda.empty_cache()
-    if rank == 0 and args.ic_compare_scale:
-        line["mixed_vs_fp64_ic"] = mixed_vs_fp64(pkg, dev, args.ic_compare_scale, 2, 1)
-        torch.cuda.empty_cache()
+    if rank == 0 and (args.compare_scale or args.ic_compare_scale):
+        # cfg3 at the comparison scale: diagonal and IC(0) preconditioning
+        same = args.compare_scale == args.ic_compare_scale
+        if args.compare_scale:
+            cmp = mixed_vs_fp64(pkg, dev, args.compare_scale, (1, 2) if same else (1,), 1)
+            line["mixed_vs_fp64"] = cmp[1]
+            if same:
+                line["mixed_vs_fp64_ic"] = cmp[2]
+            torch.cuda.empty_cache()
+        if args.ic_compare_scale and not same:
+            line["mixed_vs_fp64_ic"] = mixed_vs_fp64(pkg, dev, args.ic_compare_scale, (2,), 1)[2]
+            torch.cuda.empty_cache()
     if rank == 0 and not args.no_batch:
-        line["batched_cfg4"] = batched_cfg4(pkg, dev, 2)
+        line["batched_cfg4"] = batched_cfg4(pkg, dev, 2, autotune=not args.no_autotune)
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_cpu_baseline:
         v, n, it, el_c = cpu_reference_throughput(s, method, prec, 1, args.cpu_seconds)

@@ -63,13 +63,21 @@ typedef struct tflows_options {
                             k > 0 = k Jacobi sweeps per triangle            */
     int ic_bf16;         /* mixed + prec 2: IC off-diagonals stored in BF16 */
     double timeout_s;    /* limit for any single device-side wait           */
-    int block_size;      /* threads per block, 0 = tuned                     */
-    int grid_blocks;     /* persistent blocks, 0 = tuned                     */
+    int block_size;      /* threads per block (multiple of 32, 64..512),
+                            0 = 256 or the tuned value                      */
+    int grid_blocks;     /* persistent blocks, 0 = from rows_per_warp       */
     int device;          /* CUDA device ordinal, -1 = current                */
     int inject_stall;    /* test hook: 1 = the first block withholds its
                             arrival at the first grid barrier, so every
                             bounded wait runs out and the solve returns
                             TFLOWS_TIMEOUT (the device stays usable)        */
+    int autotune;        /* 1 = launch shapes from the tuning table, timing
+                            candidates on the first solve of a new system
+                            class (block_size and grid_blocks 0); batched
+                            launches also balance their block groups       */
+    int rows_per_warp;   /* rows each warp owns, sets the grid (0 = 32)     */
+    int sweep_warps;     /* IC sweeps: warps per chunk of the widest
+                            wavefront level (0 = 4)                         */
 } tflows_options;
 
 typedef struct tflows_result {
@@ -81,7 +89,30 @@ typedef struct tflows_result {
     double fin_res;       /* final recursive (FP64) or true (mixed) norm    */
     double seconds;       /* device time of the solve kernels               */
     double bytes;         /* algorithmic bytes moved by the solve kernels   */
+    int block_size;       /* launch shape used: threads per block           */
+    int grid_blocks;      /* blocks (batched: this system's block group)    */
+    double group_seconds; /* batched: this system's own solve time          */
 } tflows_result;
+
+/* Launch shape chosen by the autotuner for one system class. */
+typedef struct tflows_tuning {
+    int block_size;      /* threads per block                               */
+    int rows_per_warp;   /* rows per warp (0 = one 32-row slice)            */
+    int grid_blocks;     /* the grid that gives for the tuned system        */
+    int sweep_warps;     /* IC sweep warps per chunk (0 = default 4)        */
+    int candidates;      /* launch shapes timed (0 when from the table)     */
+    int from_table;      /* 1 = the table already held this class           */
+    double us_per_iteration;         /* chosen shape                        */
+    double default_us_per_iteration; /* 256 threads, one slice per warp     */
+} tflows_tuning;
+
+/* Batched-launch tuning of a plan: block size and block-group balance. */
+typedef struct tflows_batch_tuning {
+    int block_size;
+    int runs;               /* full batched solves timed                    */
+    double default_seconds; /* N^(4/3) group split, 256 threads             */
+    double tuned_seconds;   /* chosen block size and group split            */
+} tflows_batch_tuning;
 
 /* Fill *opt with the defaults (reference arithmetic and tolerance). */
 void tflows_default_options(tflows_options *opt);
@@ -189,6 +220,25 @@ int tflows_plan_create(tflows_plan **out, int count,
 int tflows_plan_launch(tflows_plan *plan, void *stream);
 int tflows_plan_results(tflows_plan *plan, tflows_result *results);
 void tflows_plan_destroy(tflows_plan *plan);
+
+/* Autotuner (no counterpart in the reference).  Times candidate launch
+ * shapes -- threads per block, rows per warp (hence the grid), IC sweep
+ * warps -- for this pattern, method, preconditioner and options on the given
+ * device values and right-hand side (capped solves from x0 = 0; x is not
+ * touched), stores the fastest per iteration in the process-wide tuning
+ * table and returns it.  The table is keyed by device, method,
+ * preconditioner, precision options and size class (quarter octaves of n);
+ * with TFLOWS_TUNE_FILE set it is read from and appended to that file.
+ * Solves with options.autotune = 1 use it. */
+int tflows_autotune(tflows_topology *topo, int method, int prec,
+                    const tflows_options *opt, const double *val,
+                    const double *b, void *stream, tflows_tuning *out);
+/* Forget every tuned entry of this process; the next lookup reads the
+ * TFLOWS_TUNE_FILE table again (the file is left as it is). */
+void tflows_autotune_clear(void);
+/* The batched-launch tuning a plan made at creation (options.autotune = 1:
+ * block size and group sizes from timed full solves). */
+int tflows_plan_tuning(const tflows_plan *plan, tflows_batch_tuning *out);
 
 /* grad_val[k] = -lambda[row(k)] * x[col(k)] over the stored pattern: the
  * gradient of a scalar loss with respect to the matrix entries, given the

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libtflows_krylov.so")
-SOURCES = ("krylov.cu", "shim.cu", "noalloc.cu")
+SOURCES = ("krylov.cu", "shim.cu", "noalloc.cu", "tune.cu")
 HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "internal.h")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -93,14 +93,37 @@ class Options(ctypes.Structure):
                 ("ic_sweeps", ctypes.c_int),
                 ("ic_bf16", ctypes.c_int), ("timeout_s", ctypes.c_double),
                 ("block_size", ctypes.c_int), ("grid_blocks", ctypes.c_int),
-                ("device", ctypes.c_int), ("inject_stall", ctypes.c_int)]
+                ("device", ctypes.c_int), ("inject_stall", ctypes.c_int),
+                ("autotune", ctypes.c_int), ("rows_per_warp", ctypes.c_int),
+                ("sweep_warps", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int),
                 ("inner_iterations", ctypes.c_int), ("refinements", ctypes.c_int),
                 ("ini_res", ctypes.c_double), ("fin_res", ctypes.c_double),
-                ("seconds", ctypes.c_double), ("bytes", ctypes.c_double)]
+                ("seconds", ctypes.c_double), ("bytes", ctypes.c_double),
+                ("block_size", ctypes.c_int), ("grid_blocks", ctypes.c_int),
+                ("group_seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("block_size", ctypes.c_int), ("rows_per_warp", ctypes.c_int),
+                ("grid_blocks", ctypes.c_int), ("sweep_warps", ctypes.c_int),
+                ("candidates", ctypes.c_int), ("from_table", ctypes.c_int),
+                ("us_per_iteration", ctypes.c_double),
+                ("default_us_per_iteration", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("block_size", ctypes.c_int), ("runs", ctypes.c_int),
+                ("default_seconds", ctypes.c_double), ("tuned_seconds", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -140,6 +163,10 @@ SIGNATURES = {
     "tflows_plan_launch": ([_VP, _VP], ctypes.c_int),
     "tflows_plan_results": ([_VP, ctypes.POINTER(Result)], ctypes.c_int),
     "tflows_plan_destroy": ([_VP], None),
+    "tflows_plan_tuning": ([_VP, ctypes.POINTER(BatchTuning)], ctypes.c_int),
+    "tflows_autotune": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Options), _VP, _VP, _VP,
+                         ctypes.POINTER(Tuning)], ctypes.c_int),
+    "tflows_autotune_clear": ([], None),
     "tflows_cg_noalloc": ([ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
                            ctypes.c_int, ctypes.c_double, _VP, _I, _D, _D], ctypes.c_int),
 }

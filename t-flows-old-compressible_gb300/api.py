@@ -82,6 +82,11 @@ def finalize() -> None:
     lib().tflows_finalize()
 
 
+def autotune_clear() -> None:
+    """Forget every tuned launch shape of this process."""
+    lib().tflows_autotune_clear()
+
+
 def _ci(a):
     a = np.ascontiguousarray(a, dtype=np.int32)
     return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
@@ -263,6 +268,21 @@ class Topology:
             raise SolverError(st, last_error())
         return res.as_dict()
 
+    def autotune(self, val, b, method="cg", prec=1, opts=None):
+        """Time candidate launch shapes on these device values and
+        right-hand side (tflows_autotune) and return the chosen one as a
+        dict; later solves of this class with ``autotune=1`` use it."""
+        for t in (val, b):
+            if not (t.is_cuda and t.dtype.itemsize == 8 and t.is_contiguous()):
+                raise TypeError("val, b must be contiguous CUDA float64 tensors")
+        out = _native.Tuning()
+        st = lib().tflows_autotune(self._h, int(METHODS.get(method, method)), int(prec),
+                                   ctypes.byref(opts) if opts else None, _ptr(val), _ptr(b),
+                                   _stream(), ctypes.byref(out))
+        if st != OK:
+            raise SolverError(st, last_error())
+        return out.as_dict()
+
     def spmv(self, val, x, y, repeat=1, fp32=False):
         sec = ctypes.c_double()
         st = lib().tflows_spmv_device(self._h, _ptr(val), _ptr(x), _ptr(y), int(repeat),
@@ -344,6 +364,15 @@ class Plan:
         res = (_native.Result * self._n)()
         lib().tflows_plan_results(self._h, res)
         return [r.as_dict() for r in res]
+
+    def tuning(self):
+        """Block size and group-balance timing the plan chose at creation
+        (options.autotune = 1); runs = 0 when it was not tuned."""
+        out = _native.BatchTuning()
+        st = lib().tflows_plan_tuning(self._h, ctypes.byref(out))
+        if st != OK:
+            raise SolverError(st, last_error())
+        return out.as_dict()
 
     def close(self):
         if self._h:

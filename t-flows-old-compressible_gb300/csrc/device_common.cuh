@@ -38,8 +38,16 @@ struct DevState {
     double ini_res;
     double fin_res;
     double bnrm2;
-    double pad[3];
+    double group_ns;     // batched launches: the system's own solve time
+    double pad[2];
 };
+
+// Nanosecond clock shared by all SMs (measurement only; waits use clock64).
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Control block shared by all blocks of one persistent launch.
 struct DevCtl {

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -32,11 +33,6 @@ struct DeviceTopology {
     int* meta = nullptr;       // n: length | diag slot << 16
     int* perm_f = nullptr;
     int* perm_b = nullptr;
-    int* chunk_lev_f = nullptr;  // level of each 32-row chunk of perm_f
-    int* chunk_lev_b = nullptr;
-    int* lev_nch_f = nullptr;    // chunks per level
-    int* lev_nch_b = nullptr;
-    unsigned* lev_cnt = nullptr; // completion counters: nlev_f forward, then nlev_b
     int* tpos = nullptr;       // transpose map (lazy)
     // host copies (0-based) for lazy derived data
     std::vector<int> h_rowptr, h_col, h_diag;
@@ -51,6 +47,7 @@ struct Workspace {
     double* sval64 = nullptr;
     float* sval32 = nullptr;
     double* svalT64 = nullptr;  // A^T values (true BiCG), allocated on first use
+    unsigned short* sval16 = nullptr;  // BF16 values for the IC sweeps (ensure_lu16)
     double* vec64 = nullptr;   // kVecs vectors of vec_cap doubles
     float* vec32 = nullptr;    // kVecs vectors of vec_cap floats
     double* csr_val = nullptr; // staging for host values (nnz)
@@ -74,11 +71,15 @@ struct SolveRequest {
     int inner_maxiter = 1000;
     int max_refinements = 30;
     int ic_sweeps = 0;
+    int ic_bf16 = 0;
     int refine_restart = 0;
     int inject_stall = 0;
     double timeout_s = 5.0;
-    int block = 0;
-    int grid = 0;
+    int block = 0;          // threads per block (0 = 256)
+    int grid = 0;           // persistent blocks (0 = from rows_per_warp)
+    int rows_per_warp = 0;  // rows each warp owns (0 = one 32-row slice)
+    int sweep_mult = 0;     // IC sweep warps per chunk of the widest level (0 = 4)
+    int autotune = 0;       // take block/rows_per_warp/sweep_mult from the tuner
 };
 
 struct SolveReport {
@@ -91,6 +92,9 @@ struct SolveReport {
     double fin_res = 0.0;
     double seconds = 0.0;
     double bytes = 0.0;
+    int block = 0;              // launch shape used
+    int grid = 0;               // blocks (batched: blocks of this system's group)
+    double group_seconds = 0.0; // batched: this system's own solve time
     std::string message;
 };
 
@@ -102,6 +106,7 @@ struct BatchSpec {
     double* x;  // workspace x (slot 11), in/out
     double* r;  // workspace residual (slot 12), holds b on entry
     SolveReport* rep;
+    double weight = 0.0;  // share of the launch's blocks (0 = N^(4/3))
 };
 
 // krylov.cu
@@ -109,7 +114,9 @@ cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t);
 void free_workspace(Workspace& ws);
 // Values (nnz FP64, stored order, device) -> SELL values (FP64 and/or FP32).
 cudaError_t permute_values(const DeviceTopology& t, Workspace& ws, const double* csr_val,
-                           bool want64, bool want32, cudaStream_t s);
+                           bool want64, bool want32, cudaStream_t s, bool want16 = false);
+// The BF16 value array of the IC sweeps (allocated once; call before a capture).
+cudaError_t ensure_lu16(Workspace& ws);
 // A^T values in A's pattern into ws.svalT64 (needs t.tpos).
 cudaError_t permute_transposed(const DeviceTopology& t, Workspace& ws, const double* csr_val,
                                cudaStream_t s);
@@ -128,14 +135,46 @@ struct BatchLaunch;
 BatchLaunch* batch_create();
 void batch_destroy(BatchLaunch* L);
 // Allocate the launch buffers for `count` systems up front (before a capture).
-cudaError_t batch_reserve(BatchLaunch* L, int count);
+cudaError_t batch_reserve(BatchLaunch* L, int count, int block = 0);
 int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s);
 int batch_collect(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s, double seconds);
 cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, double* r,
                       cudaStream_t s);
+// The grid a solve with this request would launch (co-residency included).
+int planned_grid(const DeviceTopology& t, const SolveRequest& rq);
 cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, double* y, bool fp32,
                      int repeat, cudaStream_t s, float* ms);
 cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, const double* x,
                               double* g, cudaStream_t s);
+
+// tune.cu: launch-shape autotuner.
+struct TuneChoice {
+    int block = 256;
+    int rows_per_warp = 0;
+    int grid = 0;
+    int sweep_mult = 0;
+    int candidates = 0;
+    int from_cache = 0;
+    double us_per_iter = 0.0;
+    double default_us_per_iter = 0.0;
+};
+struct BatchTuning {
+    int block = 256;
+    int runs = 0;
+    double default_seconds = 0.0;
+    double tuned_seconds = 0.0;
+};
+// The table's entry for this system class, if any.
+bool tune_lookup(const DeviceTopology& t, const SolveRequest& rq, TuneChoice& out);
+void tune_apply(const TuneChoice& ch, SolveRequest& rq);
+// Times candidate shapes on this system (values already in ws, b on the
+// device); uses workspace slots 11 and 12; stores the winner in the table.
+int tune_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, const double* b,
+               cudaStream_t s, TuneChoice& out, std::string& msg);
+void tune_clear();
+// Block size and group sizes of a batched launch from measured per-system
+// times; `restage` re-queues each system's x0 and b before every run.
+int tune_batch(std::vector<BatchSpec>& specs, const std::function<cudaError_t()>& restage,
+               cudaStream_t s, BatchTuning& out, std::string& msg);
 
 }  // namespace tflows

@@ -2,6 +2,8 @@
 #include "internal.h"
 #include "krylov_kernels.cuh"
 
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -10,13 +12,17 @@ namespace tflows {
 
 namespace {
 
+// Threads per block of the persistent kernels unless a launch asks for
+// another multiple of 32 up to kMaxBlock (the tuner's choice).  Register
+// budget: 65536 / (kBlock * kMinBlocks) per thread, i.e. kMinBlocks resident
+// blocks of kBlock threads per SM.
 constexpr int kBlock = 256;
-// Resident blocks per SM the persistent kernels are compiled for (register
-// budget 65536 / (kBlock * kMinBlocks) per thread).
+constexpr int kMaxBlock = 512;
 #ifndef TFLOWS_MINBLOCKS
 #define TFLOWS_MINBLOCKS 4
 #endif
 constexpr int kMinBlocks = TFLOWS_MINBLOCKS;
+constexpr int kMinBlocksAtMax = kMinBlocks * kBlock / kMaxBlock > 0 ? kMinBlocks * kBlock / kMaxBlock : 1;
 
 template <typename T>
 struct KParams {
@@ -44,7 +50,7 @@ __device__ int status_of(const SolveOut& o, const DevCtl* ctl) {
 
 // METHOD: 0 CG (and BiCG), 2 CGS, 9 Prec1 only.
 template <typename T, int METHOD>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) krylov_kernel(KParams<T> P) {
+__global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax) krylov_kernel(KParams<T> P) {
     Grid g;
     grid_init(g, P.ctl, P.partials, P.timeout_cyc);
     g.stall = P.stall;
@@ -97,7 +103,7 @@ struct MixedParams {
 
 // KIND: 0 restarted CG, 2 restarted CGS, 1 CG with reliable updates.
 template <int KIND>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) mixed_kernel(MixedParams P) {
+__global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax) mixed_kernel(MixedParams P) {
     Grid g;
     grid_init(g, P.ctl, P.partials, P.timeout_cyc);
     g.stall = P.stall;
@@ -156,10 +162,11 @@ __global__ void to_double_kernel(const float* __restrict__ a, double* __restrict
 
 // SELL values from stored-order values: one thread per row.  With `tpos`
 // the values of A^T in A's pattern (entry (i,j) <- stored entry (j,i)).
+// `s16` receives BF16 bit patterns, rounded to nearest even from FP64.
 __global__ void permute_kernel(int n, const int* __restrict__ rowptr,
                                const long long* __restrict__ soff, const double* __restrict__ val,
                                double* __restrict__ s64, float* __restrict__ s32,
-                               const int* __restrict__ tpos) {
+                               unsigned short* __restrict__ s16, const int* __restrict__ tpos) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int b = rowptr[i], e = rowptr[i + 1];
         const long long base = soff[i >> 5] + (i & 31);
@@ -168,6 +175,7 @@ __global__ void permute_kernel(int n, const int* __restrict__ rowptr,
             const long long o = base + 32LL * (j - b);
             if (s64) s64[o] = a;
             if (s32) s32[o] = (float)a;
+            if (s16) s16[o] = __bfloat16_as_ushort(__double2bfloat16(a));
         }
     }
 }
@@ -241,25 +249,21 @@ Mat<T> make_mat(const DeviceTopology& t, const T* sval) {
     m.meta = t.meta;
     m.perm_f = t.perm_f;
     m.perm_b = t.perm_b;
-    m.clev_f = t.chunk_lev_f;
-    m.clev_b = t.chunk_lev_b;
-    m.lnch_f = t.lev_nch_f;
-    m.lnch_b = t.lev_nch_b;
-    m.cnt_f = t.lev_cnt;
-    m.cnt_b = t.lev_cnt ? t.lev_cnt + t.nlev_f : nullptr;
+    m.lu16 = nullptr;
     m.nchunk_f = t.nchunk_f;
     m.nchunk_b = t.nchunk_b;
     m.wide_f = t.wide_f;
     m.wide_b = t.wide_b;
+    m.sweep_mult = 0;
     return m;
 }
 
-void reset_counters(const DeviceTopology& t, cudaStream_t s) {
-    if (t.lev_cnt)
-        cudaMemsetAsync(t.lev_cnt, 0, sizeof(unsigned) * (size_t)(t.nlev_f + t.nlev_b), s);
+// Blocks that give each warp `rows_per_warp` rows (rounded to whole 32-row
+// slices; 0 = one slice per warp).
+int blocks_for(int nslices, int block = kBlock, int rows_per_warp = 0) {
+    const long long per_block = (long long)std::max(1, rows_per_warp / 32) * std::max(1, block / 32);
+    return (int)std::max<long long>(1, (nslices + per_block - 1) / per_block);
 }
-
-int blocks_for(int nslices) { return std::max(1, (nslices + kBlock / 32 - 1) / (kBlock / 32)); }
 
 }  // namespace
 
@@ -280,9 +284,11 @@ cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t) {
         if (ws.sval64) cudaFree(ws.sval64);
         if (ws.sval32) cudaFree(ws.sval32);
         if (ws.svalT64) cudaFree(ws.svalT64);
+        if (ws.sval16) cudaFree(ws.sval16);
         ws.sval64 = nullptr;
         ws.sval32 = nullptr;
         ws.svalT64 = nullptr;
+        ws.sval16 = nullptr;
         if ((e = cudaMalloc(&ws.sval64, sl * sizeof(double))) != cudaSuccess) return e;
         if ((e = cudaMalloc(&ws.sval32, sl * sizeof(float))) != cudaSuccess) return e;
         ws.sell_cap = sl;
@@ -310,7 +316,8 @@ cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t) {
 
 void free_workspace(Workspace& ws) {
     for (void* p : {(void*)ws.sval64, (void*)ws.sval32, (void*)ws.vec64, (void*)ws.vec32,
-                    (void*)ws.csr_val, (void*)ws.partials, ws.ctl, ws.state, (void*)ws.svalT64})
+                    (void*)ws.csr_val, (void*)ws.partials, ws.ctl, ws.state, (void*)ws.svalT64,
+                    (void*)ws.sval16})
         if (p) cudaFree(p);
     if (ws.ev0) cudaEventDestroy(ws.ev0);
     if (ws.ev1) cudaEventDestroy(ws.ev1);
@@ -318,11 +325,18 @@ void free_workspace(Workspace& ws) {
 }
 
 cudaError_t permute_values(const DeviceTopology& t, Workspace& ws, const double* csr_val,
-                           bool want64, bool want32, cudaStream_t s) {
+                           bool want64, bool want32, cudaStream_t s, bool want16) {
+    if (want16 && !ws.sval16) return cudaErrorInvalidValue;  // ensure_lu16 first
     const int nb = std::min(std::max(1, (t.n + 255) / 256), sms() * 16);
     permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.soff, csr_val, want64 ? ws.sval64 : nullptr,
-                                      want32 ? ws.sval32 : nullptr, nullptr);
+                                      want32 ? ws.sval32 : nullptr, want16 ? ws.sval16 : nullptr,
+                                      nullptr);
     return cudaGetLastError();
+}
+
+cudaError_t ensure_lu16(Workspace& ws) {
+    if (ws.sval16) return cudaSuccess;
+    return cudaMalloc(&ws.sval16, std::max<size_t>(ws.sell_cap, 1) * sizeof(unsigned short));
 }
 
 cudaError_t permute_transposed(const DeviceTopology& t, Workspace& ws, const double* csr_val,
@@ -333,7 +347,8 @@ cudaError_t permute_transposed(const DeviceTopology& t, Workspace& ws, const dou
         if (e != cudaSuccess) return e;
     }
     const int nb = std::min(std::max(1, (t.n + 255) / 256), sms() * 16);
-    permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.soff, csr_val, ws.svalT64, nullptr, t.tpos);
+    permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.soff, csr_val, ws.svalT64, nullptr, nullptr,
+                                      t.tpos);
     return cudaGetLastError();
 }
 
@@ -355,6 +370,7 @@ Vecs<T> carve(T* base, size_t cap, T* x, T* r) {
     v.v2 = base + 8 * cap;
     v.p2 = base + 9 * cap;
     v.t = base + 10 * cap;
+    v.s = base + 13 * cap;  // FP32 only (FP64 slot 13 holds b in mixed solves)
     return v;
 }
 
@@ -366,13 +382,15 @@ int max_coresident(K kernel, int block) {
 }
 
 template <typename K, typename P>
-cudaError_t launch_coop(K kernel, P& params, int grid, cudaStream_t s) {
+cudaError_t launch_coop(K kernel, P& params, int grid, int block, cudaStream_t s) {
     void* args[] = {&params};
-    return cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(kBlock), args, 0, s);
+    return cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(block), args, 0, s);
 }
 
-int choose_grid(const DeviceTopology& t, int requested, int max_blocks) {
-    int g = requested > 0 ? requested : blocks_for(t.nslices);
+int block_of(const SolveRequest& rq) { return rq.block > 0 ? rq.block : kBlock; }
+
+int choose_grid(const DeviceTopology& t, const SolveRequest& rq, int max_blocks) {
+    int g = rq.grid > 0 ? rq.grid : blocks_for(t.nslices, block_of(rq), rq.rows_per_warp);
     return std::max(1, std::min(g, std::min(max_blocks, 64 * 1024)));
 }
 
@@ -392,10 +410,10 @@ int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, doubl
     P.timeout_cyc = timeout_cycles(timeout_s);
     P.mode = 1;
     cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
-    reset_counters(t, s);
     auto kern = krylov_kernel<double, 9>;
-    const int grid = choose_grid(t, 0, max_coresident(kern, kBlock));
-    cudaError_t e = launch_coop(kern, P, grid, s);
+    SolveRequest rq;
+    const int grid = choose_grid(t, rq, max_coresident(kern, kBlock));
+    cudaError_t e = launch_coop(kern, P, grid, kBlock, s);
     if (e != cudaSuccess) {
         rep.status = ST_CUDA_ERROR;
         rep.message = cudaGetErrorString(e);
@@ -421,6 +439,7 @@ cudaError_t prepare_fp64(const DeviceTopology& t, Workspace& ws, const SolveRequ
                          double* r, cudaStream_t s, KParams<double>& P) {
     std::memset(&P, 0, sizeof(P));
     P.m = make_mat<double>(t, ws.sval64);
+    P.m.sweep_mult = rq.sweep_mult;
     P.v = carve<double>(ws.vec64, ws.vec_cap, x, r);
     P.cfg.method = rq.method == 2 || rq.method == 3 ? rq.method : 0;
     if (rq.method == 3) P.mT = make_mat<double>(t, ws.svalT64);
@@ -437,7 +456,6 @@ cudaError_t prepare_fp64(const DeviceTopology& t, Workspace& ws, const SolveRequ
     P.mode = 0;
     P.stall = rq.inject_stall;
     cudaError_t e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
-    reset_counters(t, s);
     if (rq.prec == 2) {
         const long long nvec = (long long)t.nslices * kWarp;
         fill_sentinel_kernel<double>
@@ -453,6 +471,8 @@ cudaError_t prepare_mixed(const DeviceTopology& t, Workspace& ws, const SolveReq
     std::memset(&P, 0, sizeof(P));
     P.m64 = make_mat<double>(t, ws.sval64);
     P.m32 = make_mat<float>(t, ws.sval32);
+    P.m64.sweep_mult = rq.sweep_mult;
+    P.m32.sweep_mult = rq.sweep_mult;
     P.x64 = x;
     P.r64 = r;
     double* b64 = ws.vec64 + 13 * ws.vec_cap;
@@ -472,13 +492,17 @@ cudaError_t prepare_mixed(const DeviceTopology& t, Workspace& ws, const SolveReq
     P.cfg.inner_rtol = rq.inner_rtol > 0 ? rq.inner_rtol : 1e-1;
     P.cfg.tol_is_relative = rq.tol_relative;
     P.cfg.x_is_zero = rq.x_is_zero;
+    P.cfg.ic_sweeps = rq.prec == 2 ? std::max(rq.ic_sweeps, 0) : 0;
+    if (rq.prec == 2 && rq.ic_bf16) {
+        if (!ws.sval16) return cudaErrorInvalidValue;  // filled by permute_values
+        P.m32.lu16 = ws.sval16;
+    }
     P.ctl = (DevCtl*)ws.ctl;
     P.state = (DevState*)ws.state;
     P.partials = ws.partials;
     P.timeout_cyc = timeout_cycles(rq.timeout_s);
     P.stall = rq.inject_stall;
     if (e == cudaSuccess) e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
-    reset_counters(t, s);
     return e;
 }
 
@@ -488,15 +512,26 @@ double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevSta
     const double sl = 8.0 * (t.nslices + 1);
     const double spmv64 = (double)t.nnz * 12.0 + sl + 16.0 * t.n;
     const bool cgs = rq.method == 2;
+    // One IC(0) apply: the off-diagonal factor entries (value + index) once,
+    // the row metadata, D and the right-hand side read and the result written
+    // per triangle.  Jacobi sweeps: each sweep reads one triangle's entries.
+    const double offd = (double)std::max(0, t.nnz - t.n);
+    auto ic_bytes = [&](double sv, double sx) {
+        if (rq.precision == 1 && rq.ic_sweeps > 0)
+            return rq.ic_sweeps * (offd * (sv + 4.0) + 2.0 * t.n * (4.0 + 3.0 * sx));
+        return offd * (sv + 4.0) + 2.0 * t.n * (4.0 + 3.0 * sx);
+    };
     if (rq.precision == 1) {
         const double spmv32 = (double)t.nnz * 8.0 + sl + 8.0 * t.n;
-        const double inner_it = cgs ? 2 * spmv32 + 4.0 * t.n * 22
-                                    : spmv32 + 4.0 * t.n * (rq.prec == 1 ? 12 : 10);
+        const double ic = rq.prec == 2 ? ic_bytes(rq.ic_bf16 ? 2.0 : 4.0, 4.0) : 0.0;
+        const double inner_it = cgs ? 2 * spmv32 + 4.0 * t.n * 22 + 2 * ic
+                                    : spmv32 + 4.0 * t.n * (rq.prec == 1 ? 12 : 10) + ic;
         return inner_it * st.inner_iters + (spmv64 + 8.0 * t.n * 4) * (st.refinements + 1);
     }
     const int it = std::max(0, std::min(st.iterations, rq.maxiter));
-    const double per_it = cgs ? 2 * spmv64 + 8.0 * t.n * 22
-                              : spmv64 + 8.0 * t.n * (rq.prec == 1 ? 12 : 10);
+    const double ic = rq.prec == 2 ? ic_bytes(8.0, 8.0) : 0.0;
+    const double per_it = cgs ? 2 * spmv64 + 8.0 * t.n * 22 + 2 * ic
+                              : spmv64 + 8.0 * t.n * (rq.prec == 1 ? 12 : 10) + ic;
     return per_it * it + spmv64 + 8.0 * t.n * 4;
 }
 
@@ -518,9 +553,12 @@ void fill_report(const DeviceTopology& t, const SolveRequest& rq, const DevState
 template <typename K, typename P>
 int launch_and_report(K kern, P& params, const DeviceTopology& t, Workspace& ws,
                       const SolveRequest& rq, cudaStream_t s, SolveReport& rep, cudaError_t e) {
-    const int grid = choose_grid(t, rq.grid, max_coresident(kern, kBlock));
+    const int block = block_of(rq);
+    const int grid = choose_grid(t, rq, max_coresident(kern, block));
     cudaEventRecord(ws.ev0, s);
-    if (e == cudaSuccess) e = launch_coop(kern, params, grid, s);
+    if (e == cudaSuccess) e = launch_coop(kern, params, grid, block, s);
+    rep.block = block;
+    rep.grid = grid;
     cudaEventRecord(ws.ev1, s);
     DevState st;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ws.state, sizeof(st), cudaMemcpyDeviceToHost, s);
@@ -547,9 +585,10 @@ struct BatchItem {
 };
 
 template <int MIXED>
-__global__ void __launch_bounds__(kBlock, kMinBlocks)
+__global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax)
     batch_kernel(const BatchItem* __restrict__ items, const int* __restrict__ block_item) {
     const BatchItem& it = items[block_item[blockIdx.x]];
+    const unsigned long long t_start = globaltimer_ns();
     Grid g;
     if (!MIXED) {
         KParams<double> P = it.P64;
@@ -573,6 +612,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks)
             s->fin_res = out.fin_res;
             s->bnrm2 = out.bnrm2;
             s->timeout_where = P.ctl->where;
+            s->group_ns = (double)(globaltimer_ns() - t_start);
         }
     } else {
         MixedParams P = it.PM;
@@ -599,11 +639,27 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks)
             s->fin_res = out.fin_res;
             s->bnrm2 = out.bnrm2;
             s->timeout_where = P.ctl->where;
+            s->group_ns = (double)(globaltimer_ns() - t_start);
         }
     }
 }
 
 }  // namespace
+
+int planned_grid(const DeviceTopology& t, const SolveRequest& rq) {
+    const int block = block_of(rq);
+    int maxb;
+    if (rq.precision == 1)
+        maxb = max_coresident(rq.method == 2 ? mixed_kernel<2>
+                                             : (rq.refine_restart ? mixed_kernel<0> : mixed_kernel<1>),
+                              block);
+    else
+        maxb = max_coresident(rq.method == 2   ? krylov_kernel<double, 2>
+                              : rq.method == 3 ? krylov_kernel<double, 3>
+                                               : krylov_kernel<double, 0>,
+                              block);
+    return choose_grid(t, rq, maxb);
+}
 
 int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
               cudaStream_t s, SolveReport& rep) {
@@ -635,6 +691,7 @@ struct BatchLaunch {
     int item_cap = 0;
     int map_cap = 0;
     int total = 0;
+    int block = 0;
 };
 
 BatchLaunch* batch_create() { return new BatchLaunch(); }
@@ -686,9 +743,10 @@ void fail_all(std::vector<BatchSpec>& specs, int status, const std::string& msg)
 
 }  // namespace
 
-cudaError_t batch_reserve(BatchLaunch* L, int count) {
-    const int maxb = std::max(max_coresident(batch_kernel<0>, kBlock),
-                              max_coresident(batch_kernel<1>, kBlock));
+cudaError_t batch_reserve(BatchLaunch* L, int count, int block) {
+    if (block <= 0) block = kBlock;
+    const int maxb = std::max(max_coresident(batch_kernel<0>, block),
+                              max_coresident(batch_kernel<1>, block));
     return grow(*L, count, maxb);
 }
 
@@ -702,26 +760,34 @@ int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s)
             return ST_BAD_INPUT;
         }
     auto kern = mixed ? batch_kernel<1> : batch_kernel<0>;
-    const int maxb = max_coresident(kern, kBlock);
+    const int block = block_of(specs[0].rq);
+    for (auto& sp : specs)
+        if (block_of(sp.rq) != block) {
+            fail_all(specs, ST_BAD_INPUT, "one block size per batched launch");
+            return ST_BAD_INPUT;
+        }
+    const int maxb = max_coresident(kern, block);
     if (count > maxb) {
         fail_all(specs, ST_BAD_INPUT,
                  "more systems than co-resident blocks (" + std::to_string(maxb) + ")");
         return ST_BAD_INPUT;
     }
-    // Blocks per system in proportion to the expected work, N^(4/3) (rows
-    // times a CG iteration count growing like the mesh edge), at least one,
-    // at most one block per 8 slices.
+    // Blocks per system: the tuner's group sizes when given, else in
+    // proportion to the expected work, N^(4/3) (rows times a CG iteration
+    // count growing like the mesh edge), at least one, at most one block per
+    // rows_per_warp rows per warp (one slice per warp by default).
     std::vector<double> w(count);
     double wsum = 0.0;
     for (int k = 0; k < count; ++k) {
-        w[k] = std::pow((double)specs[k].t->n, 4.0 / 3.0);
+        w[k] = specs[k].weight > 0.0 ? specs[k].weight : std::pow((double)specs[k].t->n, 4.0 / 3.0);
         wsum += w[k];
     }
     std::vector<int> nb(count);
     int total = 0;
     for (int k = 0; k < count; ++k) {
-        const int cap = specs[k].rq.grid > 0 ? specs[k].rq.grid
-                                             : std::max(1, blocks_for(specs[k].t->nslices));
+        const int cap = specs[k].rq.grid > 0
+                            ? specs[k].rq.grid
+                            : blocks_for(specs[k].t->nslices, block, specs[k].rq.rows_per_warp);
         nb[k] = std::max(1, std::min(cap, (int)std::floor((maxb - count) * w[k] / wsum) + 1));
         total += nb[k];
     }
@@ -751,6 +817,8 @@ int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s)
         b0 += nb[k];
     }
     L->total = total;
+    L->block = block;
+    for (int k = 0; k < count; ++k) specs[k].rep->grid = nb[k];
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(L->d_items, L->h_items, sizeof(BatchItem) * count,
                             cudaMemcpyHostToDevice, s);
@@ -759,7 +827,7 @@ int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s)
     if (e == cudaSuccess) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(total);
-        cfg.blockDim = dim3(kBlock);
+        cfg.blockDim = dim3(block);
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeCooperative;
@@ -789,6 +857,8 @@ int batch_collect(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s,
     int worst = ST_OK;
     for (int k = 0; k < (int)specs.size(); ++k) {
         fill_report(*specs[k].t, specs[k].rq, L->h_state[k], seconds, *specs[k].rep);
+        specs[k].rep->block = L->block;
+        specs[k].rep->group_seconds = L->h_state[k].group_ns * 1e-9;
         worst = std::max(worst, L->h_state[k].status);
     }
     return worst;

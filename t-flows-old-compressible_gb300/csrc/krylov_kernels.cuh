@@ -30,6 +30,13 @@
 namespace tflows {
 
 constexpr double kTiny = 1.0e-64;  // Library/allp_mod.f90:31
+// TINY in the working precision: FP32 has no such number and 1e-64 rounds
+// to zero there, so the FP32 inner solves divide by D itself.
+template <typename T>
+__device__ __forceinline__ T tiny_v() {
+    if constexpr (sizeof(T) == 8) return T(kTiny);
+    else return T(0);
+}
 
 // Reduction slots in the partials array (each slot = one value per block).
 enum : int { SLOT_A = 0, SLOT_B = 4, SLOT_C = 8, SLOT_D = 12, NUM_SLOTS = 16 };
@@ -44,16 +51,14 @@ struct Mat {
     const int* __restrict__ meta;        // per row: length | diag slot << 16
     const int* __restrict__ perm_f;      // forward level order, 32-padded, -1 pads
     const int* __restrict__ perm_b;      // backward level order
-    const int* __restrict__ clev_f;      // level of each 32-row chunk
-    const int* __restrict__ clev_b;
-    const int* __restrict__ lnch_f;      // chunks per level
-    const int* __restrict__ lnch_b;
-    unsigned* cnt_f;                     // per-level completion counters
-    unsigned* cnt_b;
+    // BF16 copy of the SELL values (bit patterns), read by the IC sweeps in
+    // place of `sval` when set (the off-diagonal factor entries)
+    const unsigned short* __restrict__ lu16;
     int nchunk_f;
     int nchunk_b;
     int wide_f;  // chunks in the widest forward / backward level
     int wide_b;
+    int sweep_mult;  // sweep warps per chunk of the widest level (0 = default)
 };
 
 template <typename T>
@@ -71,6 +76,7 @@ struct Vecs {
     T* v2;
     T* p2;
     T* t;   // CGS: u1 + q1
+    T* s;   // scratch of the Jacobi-sweep IC apply (FP32 inner solves)
 };
 
 struct SolveCfg {
@@ -81,6 +87,7 @@ struct SolveCfg {
     int x_is_zero;  // skip Resid's product (x0 = 0)
     int do_prec1;   // compute D (Prec1) in this launch
     int tol_is_relative;  // tol multiplies ||b||
+    int ic_sweeps;  // prec 2: 0 = exact triangular sweeps, k > 0 = k Jacobi sweeps each
 };
 
 struct SolveOut {
@@ -202,6 +209,17 @@ __device__ __forceinline__ T sell_resid_row(const Mat<T>& m, int s, int lane, T 
     return ri;
 }
 
+// An off-diagonal factor entry for the IC sweeps: the BF16 copy when the
+// matrix carries one (FP32 inner solves with ic_bf16), else the SELL value.
+// BF16 -> FP32 is exact (the bit pattern shifted into the high half).
+template <typename T>
+__device__ __forceinline__ T lu_val(const Mat<T>& m, long long k) {
+    if constexpr (sizeof(T) == 4) {
+        if (m.lu16) return __uint_as_float((unsigned)m.lu16[k] << 16);
+    }
+    return m.sval[k];
+}
+
 template <typename T>
 __device__ __forceinline__ T diag_value(const Mat<T>& m, int i) {
     const int dslot = m.meta[i] >> 16;
@@ -223,14 +241,13 @@ constexpr int kSweepMax = 8;  // dependencies prefetched per row
 #ifndef TFLOWS_SWEEP_SLEEP
 #define TFLOWS_SWEEP_SLEEP 512
 #endif
-// Warps taking part in a sweep: no more than the widest level has chunks,
-// so each warp's next chunk is about one level ahead of the current one.
-#ifndef TFLOWS_SWEEP_WARPS_PER_CHUNK
-#define TFLOWS_SWEEP_WARPS_PER_CHUNK 4
-#endif
+// Warps taking part in a sweep: at most `per_chunk` (a tuning parameter,
+// default 4) per chunk of the widest level, so that a warp's next chunk is
+// only a few levels ahead of the front and its polls rarely spin long.
+constexpr int kSweepWarpsPerChunk = 4;
 
-__device__ __forceinline__ int sweep_warps(const Grid& g, int wide) {
-    const int want = max(1, wide * TFLOWS_SWEEP_WARPS_PER_CHUNK);
+__device__ __forceinline__ int sweep_warps(const Grid& g, int wide, int per_chunk) {
+    const int want = max(1, wide * (per_chunk > 0 ? per_chunk : kSweepWarpsPerChunk));
     return want < g.nw ? want : g.nw;
 }
 
@@ -258,7 +275,7 @@ __device__ __forceinline__ bool sweep_chunk(const Grid& g, const Mat<T>& m, int 
     for (int u = 0; u < kSweepMax; ++u) {
         const bool use = !longrow && u < n;
         c[u] = use ? m.scol[base + 32LL * (t0 + u)] : 0;
-        a[u] = use ? m.sval[base + 32LL * (t0 + u)] : T(0);
+        a[u] = use ? lu_val(m, base + 32LL * (t0 + u)) : T(0);
         v[u] = T(0);
         if (use) pending |= 1u << u;
     }
@@ -272,7 +289,7 @@ __device__ __forceinline__ bool sweep_chunk(const Grid& g, const Mat<T>& m, int 
                 while (cursor < t1) {
                     const auto b = C::load(cells + m.scol[base + 32LL * cursor]);
                     if (b == C::kSentinel) break;
-                    const T av = m.sval[base + 32LL * cursor];
+                    const T av = lu_val(m, base + 32LL * cursor);
                     const T vv = C::value(b);
                     acc = KIND == 2 ? acc - vv * av * av : acc - av * vv;
                     ++cursor;
@@ -328,7 +345,7 @@ __device__ bool prec1_phase(Grid& g, const Mat<T>& m, T* D, int prec) {
         TF_FOR_ROWS(g, m, i) { D[i] = Cell<T>::sentinel(); }
         if (!grid_sync(g, 10)) return false;
         bool ok = true;
-        const int nws = sweep_warps(g, m.wide_f);
+        const int nws = sweep_warps(g, m.wide_f, m.sweep_mult);
         for (int ch = g.wg; g.wg < nws && ch < m.nchunk_f && ok; ch += nws) {
             const int row = m.perm_f[ch * kWarp + g.lane];
             int dslot = 0;
@@ -358,7 +375,7 @@ __device__ bool prec1_phase(Grid& g, const Mat<T>& m, T* D, int prec) {
 template <typename T, typename Epi>
 __device__ bool ic_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* w, T* z, Epi epi) {
     bool ok = true;
-    const int nwf = sweep_warps(g, m.wide_f);
+    const int nwf = sweep_warps(g, m.wide_f, m.sweep_mult);
     for (int ch = g.wg; g.wg < nwf && ch < m.nchunk_f && ok; ch += nwf) {
         const int row = m.perm_f[ch * kWarp + g.lane];
         int dslot = 0;
@@ -375,7 +392,7 @@ __device__ bool ic_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* 
                             [&](T val) { Cell<T>::store(w + row, val); });
     }
     if (!grid_sync(g, 21) || !ok) return false;
-    const int nwb = sweep_warps(g, m.wide_b);
+    const int nwb = sweep_warps(g, m.wide_b, m.sweep_mult);
     for (int ch = g.wg; g.wg < nwb && ch < m.nchunk_b && ok; ch += nwb) {
         const int row = m.perm_b[ch * kWarp + g.lane];
         int dslot = 0, len = 0;
@@ -387,7 +404,7 @@ __device__ bool ic_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* 
             dslot = meta >> 16;
             base = m.soff[row >> 5] + (row & 31);
             d = D[row];
-            mid = w[row] / (d + T(kTiny));
+            mid = w[row] / (d + tiny_v<T>());
         }
         ok = sweep_chunk<1>(g, m, row, dslot + 1, row >= 0 ? len : dslot + 1, base, mid, d, z, 22,
                             [&](T zi) {
@@ -397,6 +414,99 @@ __device__ bool ic_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* 
                             });
     }
     return ok;
+}
+
+// ---- IC(0) apply by Jacobi sweeps (FP32 inner solves, ic_sweeps = k > 0) ----
+// Each triangular solve of the exact apply is replaced by k Jacobi sweeps
+//     y^s_i = D_i (f_i - sum_{t in the triangle of row i} a_it y^(s-1)_t),
+//     y^0   = D f,
+// every sweep one fully parallel pass over one triangle (no waits between
+// rows, a grid barrier between sweeps); the middle step y_i / (D_i + TINY)
+// is folded into the last forward sweep.  For a symmetric matrix the
+// backward sweeps are the transposes of the forward ones, so the operator is
+// fixed and symmetric and CG stays valid; it tends to the exact IC(0) apply
+// as k grows (after k = number of levels it is exact).
+template <bool FWD, typename T, typename Fin>
+__device__ __forceinline__ void tri_jacobi(const Grid& g, const Mat<T>& m, const T* __restrict__ D,
+                                           const T* __restrict__ f, const T* __restrict__ y,
+                                           T* __restrict__ out, Fin fin) {
+    for (int s = g.wg; s < m.nslices; s += g.nw) {
+        const int i = s * kWarp + g.lane;
+        if (i >= m.n) continue;
+        const int meta = m.meta[i];
+        const int dslot = meta >> 16;
+        const int t0 = FWD ? 0 : dslot + 1;
+        const int nt = (FWD ? dslot : (meta & 0xFFFF)) - t0;
+        const long long base = m.soff[s] + g.lane + 32LL * t0;
+        T acc = f[i];
+        const T di = D[i];
+        if (nt <= kSweepMax) {
+            int c[kSweepMax];
+            T a[kSweepMax], yv[kSweepMax];
+#pragma unroll
+            for (int u = 0; u < kSweepMax; ++u) {
+                c[u] = u < nt ? m.scol[base + 32LL * u] : 0;
+                a[u] = u < nt ? lu_val(m, base + 32LL * u) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kSweepMax; ++u)
+                yv[u] = u < nt ? (y ? y[c[u]] : D[c[u]] * f[c[u]]) : T(0);
+#pragma unroll
+            for (int u = 0; u < kSweepMax; ++u)
+                if (u < nt) acc = acc - a[u] * yv[u];
+        } else {
+            for (int u = 0; u < nt; ++u) {
+                const int c = m.scol[base + 32LL * u];
+                acc = acc - lu_val(m, base + 32LL * u) * (y ? y[c] : D[c] * f[c]);
+            }
+        }
+        out[i] = fin(i, acc * di);
+    }
+}
+
+// k forward sweeps ping-pong between w and s (the last one stores the middle
+// vector), k backward sweeps between z and the other buffer, the last one
+// into z with `epi(row, z_row)` fused.  No barrier after the last sweep.
+template <typename T, typename Epi>
+__device__ bool ic_jacobi_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* w, T* sb,
+                                T* z, int k, Epi epi) {
+    T* fb[2] = {w, sb};
+    for (int sw = 1; sw <= k; ++sw) {
+        const T* y = sw == 1 ? nullptr : fb[(sw - 1) & 1];
+        T* o = fb[sw & 1];
+        if (sw < k)
+            tri_jacobi<true>(g, m, D, rhs, y, o, [](int, T v) { return v; });
+        else
+            tri_jacobi<true>(g, m, D, rhs, y, o, [&](int i, T v) { return v / (D[i] + tiny_v<T>()); });
+        if (!grid_sync(g, 23)) return false;
+    }
+    const T* mid = fb[k & 1];
+    T* bb[2] = {z, fb[(k + 1) & 1]};
+    for (int sw = 1; sw <= k; ++sw) {
+        const T* y = sw == 1 ? nullptr : bb[(k - sw + 1) & 1];
+        T* o = bb[(k - sw) & 1];
+        if (sw < k) {
+            tri_jacobi<false>(g, m, D, mid, y, o, [](int, T v) { return v; });
+            if (!grid_sync(g, 24)) return false;
+        } else {
+            tri_jacobi<false>(g, m, D, mid, y, o, [&](int i, T v) {
+                epi(i, v);
+                return v;
+            });
+        }
+    }
+    return true;
+}
+
+// The IC(0) apply the solve was configured for: exact sync-free sweeps, or
+// `sweeps` Jacobi sweeps per triangle (FP32 inner solves only).
+template <typename T, typename Epi>
+__device__ __forceinline__ bool ic_precond(Grid& g, const Mat<T>& m, Vecs<T>& v, int sweeps,
+                                           const T* rhs, T* z, Epi epi) {
+    if constexpr (sizeof(T) == 4) {
+        if (sweeps > 0) return ic_jacobi_apply(g, m, v.D, rhs, v.w, v.s, z, sweeps, epi);
+    }
+    return ic_apply(g, m, v.D, rhs, v.w, z, epi);
 }
 
 template <typename T>
@@ -479,7 +589,7 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         if (prec == 2) {
             T a[1] = {T(0)};
             const T* rr = v.r;
-            const bool ok = ic_apply(g, m, v.D, v.r, v.w, v.z, [&](int row, T zi) {
+            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.r, v.z, [&](int row, T zi) {
                 a[0] += rr[row] * zi;
             });
             publish_t<1>(g, SLOT_A, a);
@@ -625,7 +735,7 @@ __device__ void cgs_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& 
         }
         if (!grid_sync(g, 51)) { out.exit_kind = EXIT_ABORT; return; }
         if (prec == 2) {
-            const bool ok = ic_apply(g, m, v.D, v.u2, v.w, v.p2, [](int, T) {});
+            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.u2, v.p2, [](int, T) {});
             if (!grid_sync(g, 53) || !ok) { out.exit_kind = EXIT_ABORT; return; }
         }
         // v2 = A p2; alfa = rho / (r2, v2)
@@ -671,7 +781,7 @@ __device__ void cgs_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& 
         if (!grid_sync(g, 55)) { out.exit_kind = EXIT_ABORT; return; }
         if (prec == 2) {
             T* xx = v.x;
-            const bool ok = ic_apply(g, m, v.D, v.t, v.w, v.p, [&](int row, T p1) {
+            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.t, v.p, [&](int row, T p1) {
                 xx[row] = xx[row] + alfa * p1;
             });
             if (!grid_sync(g, 57) || !ok) { out.exit_kind = EXIT_ABORT; return; }
@@ -852,6 +962,7 @@ struct MixedCfg {
     double inner_rtol;
     int tol_is_relative;
     int x_is_zero;
+    int ic_sweeps;       // prec 2: 0 exact sweeps, k > 0 Jacobi sweeps
 };
 
 struct MixedOut {
@@ -938,6 +1049,7 @@ __device__ void mixed_solve(Grid& g, const Mat<double>& m64, const Mat<float>& m
     ci.x_is_zero = 1;
     ci.do_prec1 = 0;
     ci.tol_is_relative = 1;
+    ci.ic_sweeps = c.ic_sweeps;
     int total = 0, stall = 0;
     double prev = err;
     for (int ref = 1; ref <= c.max_ref; ++ref) {
@@ -1077,7 +1189,7 @@ __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const Mat<flo
     auto ic = [&](double& rz) -> bool {
         float a[1] = {0.f};
         const float* rr = v.r;
-        const bool ok = ic_apply(g, m32, v.D, v.r, v.w, v.z, [&](int row, float zi) {
+        const bool ok = ic_precond(g, m32, v, c.ic_sweeps, v.r, v.z, [&](int row, float zi) {
             a[0] += rr[row] * zi;
         });
         publish_t<1>(g, SLOT_A, a);

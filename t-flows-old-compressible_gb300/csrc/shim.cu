@@ -75,6 +75,9 @@ void default_opts(tflows_options* o) {
     o->timeout_s = 5.0;
     o->block_size = 0;
     o->grid_blocks = 0;
+    o->autotune = 0;
+    o->rows_per_warp = 0;
+    o->sweep_warps = 0;
     o->device = -1;
 }
 
@@ -131,13 +134,9 @@ cudaError_t upload(T** dst, const T* src, size_t count) {
 
 void free_topology_arrays(DeviceTopology& t) {
     for (void* p : {(void*)t.rowptr, (void*)t.col, (void*)t.soff, (void*)t.scol, (void*)t.meta,
-                    (void*)t.perm_f, (void*)t.perm_b, (void*)t.tpos, (void*)t.chunk_lev_f,
-                    (void*)t.chunk_lev_b, (void*)t.lev_nch_f, (void*)t.lev_nch_b,
-                    (void*)t.lev_cnt})
+                    (void*)t.perm_f, (void*)t.perm_b, (void*)t.tpos})
         if (p) cudaFree(p);
     t.rowptr = t.col = t.scol = t.meta = t.perm_f = t.perm_b = t.tpos = nullptr;
-    t.chunk_lev_f = t.chunk_lev_b = t.lev_nch_f = t.lev_nch_b = nullptr;
-    t.lev_cnt = nullptr;
     t.soff = nullptr;
 }
 
@@ -177,8 +176,7 @@ cudaError_t build_levels(DeviceTopology& t) {
     if (t.levels_built) return cudaSuccess;
     const int n = t.n;
     std::vector<int> lev((size_t)n);
-    auto make_perm = [&](bool forward, int** out, int* nchunk, int* nlev, int** chunk_lev,
-                         int** lev_nch, int* wide) -> cudaError_t {
+    auto make_perm = [&](bool forward, int** out, int* nchunk, int* nlev, int* wide) -> cudaError_t {
         int maxl = -1;
         if (forward) {
             for (int i = 0; i < n; ++i) {
@@ -206,25 +204,13 @@ cudaError_t build_levels(DeviceTopology& t) {
         for (int i = 0; i < n; ++i) perm[fill[lev[i]]++] = i;
         *nchunk = (int)(start[L] / 32);
         *nlev = L;
-        std::vector<int> clev((size_t)std::max(*nchunk, 1), 0), nch((size_t)L, 0);
         *wide = 0;
-        for (int l = 0; l < L; ++l) {
-            nch[l] = (int)((start[l + 1] - start[l]) / 32);
-            *wide = std::max(*wide, nch[l]);
-            for (long long c = start[l] / 32; c < start[l + 1] / 32; ++c) clev[c] = l;
-        }
-        cudaError_t e = upload(out, perm.data(), perm.size());
-        if (e == cudaSuccess) e = upload(chunk_lev, clev.data(), clev.size());
-        if (e == cudaSuccess) e = upload(lev_nch, nch.data(), nch.size());
-        return e;
+        for (int l = 0; l < L; ++l) *wide = std::max(*wide, (int)((start[l + 1] - start[l]) / 32));
+        return upload(out, perm.data(), perm.size());
     };
-    cudaError_t e = make_perm(true, &t.perm_f, &t.nchunk_f, &t.nlev_f, &t.chunk_lev_f, &t.lev_nch_f,
-                              &t.wide_f);
+    cudaError_t e = make_perm(true, &t.perm_f, &t.nchunk_f, &t.nlev_f, &t.wide_f);
     if (e != cudaSuccess) return e;
-    e = make_perm(false, &t.perm_b, &t.nchunk_b, &t.nlev_b, &t.chunk_lev_b, &t.lev_nch_b,
-                  &t.wide_b);
-    if (e != cudaSuccess) return e;
-    e = cudaMalloc(&t.lev_cnt, sizeof(unsigned) * (size_t)(t.nlev_f + t.nlev_b));
+    e = make_perm(false, &t.perm_b, &t.nchunk_b, &t.nlev_b, &t.wide_b);
     if (e != cudaSuccess) return e;
     t.levels_built = true;
     return cudaSuccess;
@@ -372,13 +358,62 @@ SolveRequest make_request(const tflows_options& o, int method, int prec, int max
     rq.inner_rtol = o.inner_rtol;
     rq.inner_maxiter = o.inner_maxiter;
     rq.max_refinements = o.max_refinements;
-    rq.ic_sweeps = o.ic_sweeps;
+    // Jacobi sweeps and BF16 factor values exist only in the FP32 inner
+    // solves of the mixed mode with IC(0).
+    const bool mixed_ic = o.precision == TFLOWS_MIXED && prec == 2;
+    rq.ic_sweeps = mixed_ic ? std::max(o.ic_sweeps, 0) : 0;
+    rq.ic_bf16 = mixed_ic && o.ic_bf16 ? 1 : 0;
     rq.refine_restart = o.refine_restart;
     rq.inject_stall = o.inject_stall;
     rq.timeout_s = o.timeout_s > 0 ? o.timeout_s : 5.0;
     rq.block = o.block_size;
     rq.grid = o.grid_blocks;
+    rq.rows_per_warp = o.rows_per_warp;
+    rq.sweep_mult = o.sweep_warps;
+    rq.autotune = o.autotune && o.block_size == 0 && o.grid_blocks == 0 ? 1 : 0;
     return rq;
+}
+
+// Launch-shape options a kernel launch can take.
+bool shape_ok(const SolveRequest& rq, std::string& msg) {
+    if (rq.block != 0 && (rq.block % 32 != 0 || rq.block < 64 || rq.block > 512)) {
+        msg = "block_size must be 0 or a multiple of 32 in 64..512";
+        return false;
+    }
+    if (rq.grid < 0 || rq.rows_per_warp < 0 || rq.sweep_mult < 0) {
+        msg = "grid_blocks, rows_per_warp and sweep_warps must be >= 0";
+        return false;
+    }
+    return true;
+}
+
+// The tuned launch shape for this system class: from the table, or timed
+// now on the caller's values and right-hand side (device arrays; x0 and b
+// are preserved even where they live in the workspace slots the timing
+// runs use).
+int autotune_on(tflows_topology* tp, SolveRequest& rq, const double* d_b, const double* d_x,
+                cudaStream_t s, TuneChoice& ch) {
+    if (tune_lookup(tp->t, rq, ch)) {
+        tune_apply(ch, rq);
+        return TFLOWS_OK;
+    }
+    const size_t nb = sizeof(double) * tp->t.n;
+    double* tmp = nullptr;
+    cudaError_t e = cudaMalloc(&tmp, 2 * std::max<size_t>(nb, 8));
+    if (e != cudaSuccess) return cuda_fail(e, "tuning buffers");
+    double* tb = tmp;
+    double* tx = tmp + std::max<size_t>(tp->t.n, 1);
+    e = cudaMemcpyAsync(tb, d_b, nb, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && d_x) e = cudaMemcpyAsync(tx, d_x, nb, cudaMemcpyDeviceToDevice, s);
+    std::string msg;
+    int st = e == cudaSuccess ? tune_solve(tp->t, tp->ws, rq, tb, s, ch, msg) : TFLOWS_CUDA_ERROR;
+    if (e == cudaSuccess && d_x) e = cudaMemcpyAsync((double*)d_x, tx, nb, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail(e, "tuning");
+    if (st != TFLOWS_OK) return fail(st, msg);
+    tune_apply(ch, rq);
+    return TFLOWS_OK;
 }
 
 void record(const SolveReport& rep, tflows_result* res) {
@@ -391,6 +426,9 @@ void record(const SolveReport& rep, tflows_result* res) {
     r.fin_res = rep.fin_res;
     r.seconds = rep.seconds;
     r.bytes = rep.bytes;
+    r.block_size = rep.block;
+    r.grid_blocks = rep.grid;
+    r.group_seconds = rep.group_seconds;
     t_result = r;
     if (res) *res = r;
 }
@@ -400,6 +438,7 @@ void record(const SolveReport& rep, tflows_result* res) {
 int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, const double* d_b,
              double* d_x, double* d_r_out, cudaStream_t s, SolveReport& rep) {
     SolveRequest rq = rq0;
+    if (std::string msg; !shape_ok(rq, msg)) return fail(TFLOWS_BAD_INPUT, msg);
     if (rq.method == TFLOWS_METHOD_BICG_TRUE) {
         if (rq.precision != TFLOWS_FP64)
             return fail(TFLOWS_UNSUPPORTED, "true BiCG runs in FP64 only");
@@ -418,12 +457,18 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
         if (e != cudaSuccess) return cuda_fail(e, "level sets");
     }
     cudaError_t e = ensure_workspace(tp->ws, tp->t);
+    if (e == cudaSuccess && rq.ic_bf16) e = ensure_lu16(tp->ws);
     if (e != cudaSuccess) return cuda_fail(e, "workspace");
-    if ((e = permute_values(tp->t, tp->ws, d_val, true, rq.precision != TFLOWS_FP64, s)) != cudaSuccess)
+    if ((e = permute_values(tp->t, tp->ws, d_val, true, rq.precision != TFLOWS_FP64, s,
+                            rq.ic_bf16 != 0)) != cudaSuccess)
         return cuda_fail(e, "value layout");
     if (rq.method == TFLOWS_METHOD_BICG_TRUE &&
         (e = permute_transposed(tp->t, tp->ws, d_val, s)) != cudaSuccess)
         return cuda_fail(e, "transposed values");
+    if (rq.autotune) {
+        TuneChoice ch;
+        if (int st = autotune_on(tp, rq, d_b, d_x, s, ch); st != TFLOWS_OK) return st;
+    }
     // The kernels work on padded, 16-byte aligned workspace vectors: x and b
     // are staged into workspace slots 11 and 12 unless they already are them.
     const size_t nb = sizeof(double) * tp->t.n;
@@ -783,6 +828,7 @@ int tflows_solve_batched_device(int count, tflows_topology* const* topos, const 
         while ((int)tp->extra_ws.size() < j) tp->extra_ws.emplace_back(new Workspace());
         Workspace* ws = j == 0 ? &tp->ws : tp->extra_ws[j - 1].get();
         SolveRequest rq = make_request(o, methods[k], precs[k], maxiters[k], tols[k]);
+        if (std::string msg; !shape_ok(rq, msg)) return fail(TFLOWS_BAD_INPUT, msg);
         if (rq.method == TFLOWS_METHOD_BICG_TRUE)
             return fail(TFLOWS_UNSUPPORTED, "true BiCG is not available in batched solves");
         if (rq.prec == 2) {
@@ -791,7 +837,10 @@ int tflows_solve_batched_device(int count, tflows_topology* const* topos, const 
             if (e != cudaSuccess) return cuda_fail(e, "level sets");
         }
         cudaError_t e = ensure_workspace(*ws, tp->t);
-        if (e == cudaSuccess) e = permute_values(tp->t, *ws, vals[k], true, rq.precision != TFLOWS_FP64, s);
+        if (e == cudaSuccess && rq.ic_bf16) e = ensure_lu16(*ws);
+        if (e == cudaSuccess)
+            e = permute_values(tp->t, *ws, vals[k], true, rq.precision != TFLOWS_FP64, s,
+                               rq.ic_bf16 != 0);
         double* X = ws->vec64 + 11 * ws->vec_cap;
         double* R = ws->vec64 + 12 * ws->vec_cap;
         const size_t nb = sizeof(double) * tp->t.n;
@@ -836,6 +885,8 @@ struct tflows_plan {
     cudaGraphExec_t exec = nullptr;
     cudaStream_t last = nullptr;
     int device = 0;
+    BatchTuning tuning;
+    bool tuned = false;
 };
 
 int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* topos,
@@ -860,6 +911,7 @@ int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* top
         if (tp->t.device != plan->device) return fail(TFLOWS_BAD_INPUT, "systems on different devices");
         std::lock_guard<std::mutex> lk(tp->mu);
         SolveRequest rq = make_request(o, methods[k], precs[k], maxiters[k], tols[k]);
+        if (std::string msg; !shape_ok(rq, msg)) return fail(TFLOWS_BAD_INPUT, msg);
         if (rq.method == TFLOWS_METHOD_BICG_TRUE)
             return fail(TFLOWS_UNSUPPORTED, "true BiCG is not available in batched solves");
         if (rq.prec == 2) {
@@ -867,8 +919,9 @@ int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* top
             if (cudaError_t e = build_levels(tp->t); e != cudaSuccess) return cuda_fail(e, "level sets");
         }
         plan->ws.emplace_back(new Workspace());
-        if (cudaError_t e = ensure_workspace(*plan->ws.back(), tp->t); e != cudaSuccess)
-            return cuda_fail(e, "workspace");
+        cudaError_t ew = ensure_workspace(*plan->ws.back(), tp->t);
+        if (ew == cudaSuccess && rq.ic_bf16) ew = ensure_lu16(*plan->ws.back());
+        if (ew != cudaSuccess) return cuda_fail(ew, "workspace");
         Workspace* ws = plan->ws.back().get();
         plan->specs[k] = BatchSpec{&tp->t, ws, rq, ws->vec64 + 11 * ws->vec_cap,
                                    ws->vec64 + 12 * ws->vec_cap, &plan->reps[k]};
@@ -876,8 +929,34 @@ int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* top
     }
     cudaError_t e = cudaStreamCreateWithFlags(&plan->cap, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_fail(e, "plan stream");
+    if (o.autotune && o.block_size == 0 && o.grid_blocks == 0) {
+        // Block size and group split from timed full batched solves on the
+        // caller's data (x0 and b re-staged before every run).
+        cudaStream_t ts = plan->cap;
+        for (int k = 0; k < count && e == cudaSuccess; ++k) {
+            BatchSpec& sp = plan->specs[k];
+            e = permute_values(*sp.t, *sp.ws, vals[k], true, sp.rq.precision != TFLOWS_FP64, ts,
+                               sp.rq.ic_bf16 != 0);
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "plan tuning");
+        auto restage = [&]() -> cudaError_t {
+            cudaError_t er = cudaSuccess;
+            for (int k = 0; k < count && er == cudaSuccess; ++k) {
+                BatchSpec& sp = plan->specs[k];
+                const size_t nb = sizeof(double) * sp.t->n;
+                er = cudaMemcpyAsync(sp.x, xs[k], nb, cudaMemcpyDeviceToDevice, ts);
+                if (er == cudaSuccess) er = cudaMemcpyAsync(sp.r, bs[k], nb, cudaMemcpyDeviceToDevice, ts);
+            }
+            return er;
+        };
+        std::string msg;
+        const int st = tune_batch(plan->specs, restage, ts, plan->tuning, msg);
+        if (st != TFLOWS_OK) return fail(st, msg);
+        plan->tuned = true;
+        for (auto& r : plan->reps) r = SolveReport();
+    }
     plan->launch = batch_create();
-    if ((e = batch_reserve(plan->launch, count)) != cudaSuccess) {
+    if ((e = batch_reserve(plan->launch, count, plan->specs[0].rq.block)) != cudaSuccess) {
         tflows_plan_destroy(plan.release());
         return cuda_fail(e, "plan buffers");
     }
@@ -888,7 +967,8 @@ int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* top
     for (int k = 0; k < count && e == cudaSuccess; ++k) {
         BatchSpec& sp = plan->specs[k];
         const size_t nb = sizeof(double) * sp.t->n;
-        e = permute_values(*sp.t, *sp.ws, vals[k], true, sp.rq.precision != TFLOWS_FP64, s);
+        e = permute_values(*sp.t, *sp.ws, vals[k], true, sp.rq.precision != TFLOWS_FP64, s,
+                           sp.rq.ic_bf16 != 0);
         if (e == cudaSuccess) e = cudaMemcpyAsync(sp.x, xs[k], nb, cudaMemcpyDeviceToDevice, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(sp.r, bs[k], nb, cudaMemcpyDeviceToDevice, s);
     }
@@ -943,6 +1023,57 @@ void tflows_plan_destroy(tflows_plan* plan) {
     for (auto& w : plan->ws) free_workspace(*w);
     delete plan;
 }
+
+int tflows_plan_tuning(const tflows_plan* plan, tflows_batch_tuning* out) {
+    if (!plan || !out) return fail(TFLOWS_BAD_INPUT, "null argument");
+    out->block_size = plan->specs.empty() ? 0 : std::max(plan->specs[0].rq.block, 0);
+    if (out->block_size == 0) out->block_size = 256;
+    out->runs = plan->tuned ? plan->tuning.runs : 0;
+    out->default_seconds = plan->tuned ? plan->tuning.default_seconds : 0.0;
+    out->tuned_seconds = plan->tuned ? plan->tuning.tuned_seconds : 0.0;
+    return TFLOWS_OK;
+}
+
+int tflows_autotune(tflows_topology* topo, int method, int prec, const tflows_options* opt,
+                    const double* val, const double* b, void* stream, tflows_tuning* out) {
+    t_error.clear();
+    if (!topo || !val || !b || !out) return fail(TFLOWS_BAD_INPUT, "null argument");
+    tflows_options o;
+    if (opt) o = *opt;
+    else default_opts(&o);
+    std::lock_guard<std::mutex> lk(topo->mu);
+    cudaSetDevice(topo->t.device);
+    SolveRequest rq = make_request(o, method, prec, 1, 0.0);
+    if (std::string msg; !shape_ok(rq, msg)) return fail(TFLOWS_BAD_INPUT, msg);
+    if (rq.method == TFLOWS_METHOD_BICG_TRUE)
+        return fail(TFLOWS_UNSUPPORTED, "the tuner covers CG, BiCG and CGS");
+    if (rq.prec == 2) {
+        if (!topo->t.ic_ok) return fail(TFLOWS_BAD_INPUT, "IC(0) needs a triangular-ordered pattern");
+        if (cudaError_t e = build_levels(topo->t); e != cudaSuccess) return cuda_fail(e, "level sets");
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = ensure_workspace(topo->ws, topo->t);
+    if (e == cudaSuccess && rq.ic_bf16) e = ensure_lu16(topo->ws);
+    if (e == cudaSuccess)
+        e = permute_values(topo->t, topo->ws, val, true, rq.precision != TFLOWS_FP64, s,
+                           rq.ic_bf16 != 0);
+    if (e != cudaSuccess) return cuda_fail(e, "tuning setup");
+    TuneChoice ch;
+    const int st = autotune_on(topo, rq, b, nullptr, s, ch);
+    if (st != TFLOWS_OK) return st;
+    out->block_size = ch.block;
+    out->rows_per_warp = ch.rows_per_warp;
+    out->grid_blocks = planned_grid(topo->t, rq);
+    out->sweep_warps = ch.sweep_mult;
+    out->candidates = ch.candidates;
+    out->from_table = ch.from_cache;
+    out->us_per_iteration = ch.us_per_iter;
+    out->default_us_per_iteration = ch.default_us_per_iter;
+    t_status = TFLOWS_OK;
+    return TFLOWS_OK;
+}
+
+void tflows_autotune_clear(void) { tune_clear(); }
 
 int tflows_pattern_outer(tflows_topology* topo, const double* lambda, const double* x,
                          double* grad_val, void* stream) {

@@ -30,11 +30,11 @@ def _dev(a):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_batched_matches_one_at_a_time(precision):
+@pytest.mark.parametrize("precision,ic", [(0, {}), (1, {}), (1, {"ic_bf16": 1, "ic_sweeps": 2})])
+def test_batched_matches_one_at_a_time(precision, ic):
     import torch
     systems = _systems()
-    opts = tflows.options(precision=precision)
+    opts = tflows.options(precision=precision, **ic)
     topos = [tflows.Topology.from_system(s) for s, _, _ in systems]
     vals = [_dev(s.A[:-1]) for s, _, _ in systems]
     bs = [_dev(s.b) for s, _, _ in systems]

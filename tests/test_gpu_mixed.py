@@ -74,3 +74,39 @@ def test_mixed_divergent_inner_solve_is_rejected():
     assert out.status in (tflows.OK, tflows.NOT_CONVERGED, tflows.NONFINITE)
     if out.status != tflows.OK:
         assert np.isfinite(out.FinRes) and out.FinRes <= out.IniRes * 1.0001
+
+
+@pytest.mark.parametrize("method", ["cg", "cgs"])
+@pytest.mark.parametrize("sweeps,bf16", [(0, 1), (1, 0), (2, 1), (3, 0)])
+def test_mixed_ic_variants_reach_fp64_tolerance(method, sweeps, bf16):
+    """IC(0) in the FP32 inner solves with BF16 factor entries and/or Jacobi
+    sweeps in place of the exact triangular solves: a different (cheaper)
+    preconditioner, the same FP64 answer."""
+    if method == "cg":
+        s = mesh.pressure_system(20, 18, 16, perturb=0.2, seed=11, variable_density=True)
+    else:
+        s = mesh.convection_diffusion_system(24, 20, 18, perturb=0.2, seed=5)
+    x, r, out, tol, res = _mixed(s, method, 2, 1e-10, ic_sweeps=sweeps, ic_bf16=bf16)
+    assert out.status == tflows.OK, (out, res)
+    true_r = s.b - s.scipy() @ x[s.NB + 1:]
+    assert np.linalg.norm(true_r) < tol
+    xo, *_ = oracle.solve(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab, s.x,
+                          s.b, 2, 5000, tol)
+    assert np.abs(x - xo).max() / np.abs(xo).max() < 1e-6
+
+
+def test_ic_jacobi_sweeps_tend_to_the_exact_apply():
+    """With at least as many Jacobi sweeps as the triangles have wavefront
+    levels the sweeps reproduce the exact triangular solves (up to FP32
+    rounding), so the inner iteration count matches the exact apply's; with
+    fewer sweeps the preconditioner is weaker but still converges."""
+    s = mesh.pressure_system(6, 5, 4, perturb=0.2, seed=8, variable_density=True)
+    levels = 6 + 5 + 4 - 2  # a box's IC wavefronts: nx + ny + nz - 2
+    runs = {}
+    for k in (0, levels + 1, 1):
+        x, r, out, tol, res = _mixed(s, "cg", 2, 1e-11, ic_sweeps=k, inner_rtol=1e-6,
+                                     refine_restart=1)
+        assert out.status == tflows.OK, (k, out, res)
+        runs[k] = res["inner_iterations"]
+    assert abs(runs[levels + 1] - runs[0]) <= 1, runs
+    assert runs[1] >= runs[0], runs
