@@ -318,6 +318,136 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
             "gbs": byts / (ms * 1e-3) / 1e9}
 
 
+def cfg2_methods(pkg, dev, topo, s, val, b, reps=3):
+    """The other config-2 solvers on the same 128^3 system: CGS (FP64), the
+    true-BiCG extension (shadow sequence with A^T, FP64) and BiCG in mixed
+    precision, each to the same absolute tolerance from x0 = 0."""
+    import torch
+    x = torch.zeros(s.N, dtype=torch.float64, device=dev)
+    out = {}
+    for label, method, precision in (("cgs_fp64", "cgs", pkg.FP64),
+                                     ("bicg_true_fp64", "bicg_true", pkg.FP64),
+                                     ("bicg_mixed", "bicg", pkg.MIXED)):
+        opts = pkg.options(precision=precision)
+        el, res = device_solves(pkg, topo, val, b, x, method, 1, s.tol, opts, reps, 1)
+        r = res[-1]
+        out[label] = {"ms": 1e3 * el / reps, "solves_per_s": reps / el,
+                      "iterations": r["iterations"], "status": r["status"],
+                      "gbs": r["bytes"] / r["seconds"] / 1e9, "fin_res": r["fin_res"]}
+    return out
+
+
+def adjoint_cfg5(pkg, dev, reps=3):
+    """Config 5: 64^3 variable-density pressure assembled differentiably from
+    its float32 face coefficients, loss 0.5||x - x_t||^2, one forward solve
+    and one backward (transposed) solve per step; gradients with respect to
+    b (float64) and the coefficients (float32)."""
+    import numpy as np
+    import torch
+    from tflows_gb300 import autograd as ag
+    s = pkg.mesh.pressure_system(64, 64, 64, perturb=0.2, seed=0, variable_density=True,
+                                 keep_faces=True)
+    solver = ag.DifferentiableSolver.from_system(s, method="cg", prec=1, rtol=1e-10)
+    asm = ag.FaceAssembly(s, device=dev)
+    xt = torch.as_tensor(np.random.default_rng(100).uniform(-1, 1, s.N), device=dev)
+    coef = torch.tensor(s.face_coef, dtype=torch.float32, device=dev, requires_grad=True)
+    b = torch.tensor(s.b, dtype=torch.float64, device=dev, requires_grad=True)
+
+    def step():
+        coef.grad = None
+        b.grad = None
+        x = solver(asm(coef), b)
+        loss = 0.5 * ((x - xt) ** 2).sum()
+        loss.backward()
+        return loss
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    fw, bw = solver.last_forward, solver.last_adjoint
+    solver.topo.close()
+    return {"workload": f"{s.name} differentiable CG + diagonal, rtol 1e-10, loss 0.5||x-x_t||^2",
+            "n": s.N, "ms_per_forward_backward": ms,
+            "forward": {"iterations": fw["iterations"], "ms": 1e3 * fw["seconds"]},
+            "adjoint": {"iterations": bw["iterations"], "ms": 1e3 * bw["seconds"]},
+            "grad_b_norm": float(b.grad.norm()), "grad_coef_norm": float(coef.grad.norm())}
+
+
+def simple_step(pkg, dev, n=128, reps=3, autotune=True):
+    """The five solves of one SIMPLE outer iteration on one 128^3 mesh (one
+    topology): mixture fraction (cg, Process/CalcZmix.f90:394), three momentum
+    components (bicg, NewUVW.f90:506) and the pressure correction (cg,
+    CalcPS.f90:217), FP64 with diagonal preconditioning, each to 1e-8*||b||
+    absolute; one graph-captured persistent launch per step against five
+    consecutive single-system solves."""
+    import numpy as np
+    import torch
+    cd = pkg.mesh.convection_diffusion_system(n, n, n, perturb=0.2, seed=21)
+    zm = pkg.mesh.convection_diffusion_system(n, n, n, perturb=0.2, seed=22)
+    pr = pkg.mesh.pressure_system(n, n, n, perturb=0.2, seed=23, variable_density=True)
+    assert np.array_equal(cd.Arow, pr.Arow) and np.array_equal(cd.Acol, pr.Acol)
+    topo = pkg.Topology.from_system(pr)
+    rng = np.random.default_rng(24)
+    mom = [torch.from_numpy(cd.b * (1.0 + 0.1 * k) + rng.uniform(-0.1, 0.1, cd.N)).to(dev)
+           for k in range(3)]
+    systems = [(zm, torch.from_numpy(zm.b.copy()).to(dev), "cg")] + \
+              [(cd, bk, "bicg") for bk in mom] + \
+              [(pr, torch.from_numpy(pr.b.copy()).to(dev), "cg")]
+    vals = {id(m): torch.from_numpy(m.A[:-1].copy()).to(dev) for m in (cd, zm, pr)}
+    vs = [vals[id(m)] for m, _, _ in systems]
+    bs = [bk for _, bk, _ in systems]
+    tols = [1e-8 * float(bk.norm()) for bk in bs]
+    xs = [torch.zeros(pr.N, dtype=torch.float64, device=dev) for _ in systems]
+    opts = pkg.options(autotune=int(autotune))
+    plan = pkg.Plan([topo] * 5, vs, bs, xs, [m for _, _, m in systems], [1] * 5, [20000] * 5,
+                    tols, opts)
+    tuning = plan.tuning()
+    plan.launch()
+    plan.results()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        for x in xs:
+            x.zero_()
+        plan.launch()
+    e1.record()
+    res = plan.results()
+    torch.cuda.synchronize()
+    plan_ms = e0.elapsed_time(e1) / reps
+    seq = pkg.options()
+    x = torch.zeros(pr.N, dtype=torch.float64, device=dev)
+    for _ in range(1):
+        for (m, bk, meth), v, tl in zip(systems, vs, tols):
+            x.zero_()
+            topo.solve(v, bk, x, meth, 1, 20000, tl, opts=seq)
+    torch.cuda.synchronize()
+    e0.record()
+    seq_res = []
+    for _ in range(reps):
+        for (m, bk, meth), v, tl in zip(systems, vs, tols):
+            x.zero_()
+            seq_res.append(topo.solve(v, bk, x, meth, 1, 20000, tl, opts=seq))
+    e1.record()
+    torch.cuda.synchronize()
+    seq_ms = e0.elapsed_time(e1) / reps
+    plan.close()
+    topo.close()
+    return {"workload": f"SIMPLE step on {n}^3 (one topology): Zmix cg, 3x momentum bicg, "
+                        "pressure cg, prec 1, FP64, tol 1e-8*||b||",
+            "plan_ms": plan_ms, "sequential_ms": seq_ms, "speedup": seq_ms / plan_ms,
+            "iterations": [r["iterations"] for r in res],
+            "converged": sum(1 for r in res if r["status"] == pkg.OK),
+            "group_blocks": [r["grid_blocks"] for r in res], "tuning": tuning}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -335,6 +465,8 @@ def main():
                     help="edge of the cfg3 mixed-vs-FP64 comparison (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (cfg4) block")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the config-2 method, config-5 adjoint and SIMPLE-step blocks")
     ap.add_argument("--no-autotune", action="store_true",
                     help="fixed launch shape (256 threads, one slice per warp)")
     ap.add_argument("--ic-compare-scale", type=int, default=256,
@@ -452,9 +584,17 @@ def main():
                      "bytes": byts}
     line["clocks"] = clk
     line["gpu_launches"] = 2 * args.steps
+    x_gpu = x.cpu().numpy()
+    if rank == 0 and not args.no_extras:
+        line["cfg2_methods"] = cfg2_methods(pkg, dev, topo, s, val, b)
     topo.close()
     del val, b, x, y, xs
     torch.cuda.empty_cache()
+    if rank == 0 and not args.no_extras:
+        line["adjoint_cfg5"] = adjoint_cfg5(pkg, dev)
+        torch.cuda.empty_cache()
+        line["simple_step"] = simple_step(pkg, dev, autotune=not args.no_autotune)
+        torch.cuda.empty_cache()
 
     if rank == 0 and (args.compare_scale or args.ic_compare_scale):
         # cfg3 at the comparison scale: diagonal and IC(0) preconditioning
@@ -477,6 +617,13 @@ def main():
                                 "sample": f"{n} full {method} solves ({it} iterations) of the "
                                           f"same system, oracle C restatement, 1 thread, "
                                           f"{el_c:.1f} s"}
+        # the GPU answer against the CPU restatement of the reference
+        import oracle
+        xo, _, it_o, _, _ = oracle.solve(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia,
+                                         s.Ab, s.x, s.b, prec, 20000, tol)
+        xo = xo[s.NB + 1:]
+        line["rel_err_vs_oracle"] = float(np.abs(x_gpu - xo).max() / np.abs(xo).max())
+        line["oracle_iterations"] = int(it_o)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -102,3 +102,43 @@ def test_graph_plan_replays_with_new_data(precision):
             x = xs[k].cpu().numpy()
             assert np.linalg.norm(rhs[k] - s.scipy() @ x) < 2e-10 * np.linalg.norm(rhs[k]), (step, k)
     plan.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_simple_step_plan_on_one_topology(precision):
+    """The five solves of one SIMPLE outer iteration -- mixture fraction (cg),
+    three momentum components (bicg) and pressure correction (cg, IC) -- on
+    one mesh topology, replayed from one captured plan; each system must
+    match its own single-system solve."""
+    import torch
+    cd = mesh.convection_diffusion_system(14, 12, 10, perturb=0.2, seed=21)
+    zm = mesh.convection_diffusion_system(14, 12, 10, perturb=0.2, seed=22)
+    pr = mesh.pressure_system(14, 12, 10, perturb=0.2, seed=23, variable_density=True)
+    topo = tflows.Topology.from_system(pr)
+    rng = np.random.default_rng(24)
+    rhs = [zm.b] + [cd.b * (1.0 + 0.1 * k) + rng.uniform(-0.1, 0.1, cd.N) for k in range(3)] + [pr.b]
+    mats = [zm, cd, cd, cd, pr]
+    methods = ["cg", "bicg", "bicg", "bicg", "cg"]
+    precs = [1, 1, 1, 1, 2]
+    vals = [_dev(m.A[:-1]) for m in mats]
+    bs = [_dev(b) for b in rhs]
+    xs = [torch.zeros(pr.N, dtype=torch.float64, device="cuda") for _ in mats]
+    tols = [1e-10 * float(np.linalg.norm(b)) for b in rhs]
+    opts = tflows.options(precision=precision)
+    plan = tflows.Plan([topo] * 5, vals, bs, xs, methods, precs, [3000] * 5, tols, opts)
+    for _ in range(2):
+        for x in xs:
+            x.zero_()
+        plan.launch()
+        res = plan.results()
+        for k in range(5):
+            assert res[k]["status"] == tflows.OK, (k, res[k])
+            x1 = torch.zeros(pr.N, dtype=torch.float64, device="cuda")
+            r1 = topo.solve(vals[k], bs[k], x1, methods[k], precs[k], 3000, tols[k], opts=opts)
+            assert r1["status"] == tflows.OK
+            assert abs(res[k]["iterations"] - r1["iterations"]) <= 2, (k, res[k], r1)
+            xa, xb = xs[k].cpu().numpy(), x1.cpu().numpy()
+            assert np.abs(xa - xb).max() <= 1e-7 * np.abs(xb).max(), k
+            assert np.linalg.norm(rhs[k] - mats[k].scipy() @ xa) < 2 * tols[k]
+    plan.close()
+    topo.close()
