@@ -239,17 +239,26 @@ unsigned long long mix(unsigned long long h, unsigned long long v) {
 }
 
 // Hash of the pattern arrays: every element when TFLOWS_TOPOLOGY_CHECK=full,
-// otherwise ~64k samples spread over each array plus both ends.
+// otherwise ~8k samples spread over each array plus both ends.
 unsigned long long pattern_hash(int n, int nnz, const int* Acol, const int* Arow, const int* Adia) {
     static const bool full = [] {
         const char* v = std::getenv("TFLOWS_TOPOLOGY_CHECK");
         return v && std::strcmp(v, "full") == 0;
     }();
     unsigned long long h = mix(0x1234567ull, (unsigned long long)n * 1000003ull + nnz);
+    // About 8k evenly spaced entries per array (every entry with "full"),
+    // hashed into four independent chains so that the loads overlap: the
+    // check costs tens of microseconds per call, not milliseconds.
     auto sample = [&](const int* a, long long len) {
         if (len <= 0) return;
-        const long long step = full ? 1 : std::max(1LL, len / 65536);
-        for (long long i = 0; i < len; i += step) h = mix(h, (unsigned)a[i] + (unsigned long long)i * 31);
+        const long long step = full ? 1 : std::max(1LL, len / 8192);
+        unsigned long long c[4] = {h, h ^ 0x9e37ull, h ^ 0x7f4aull, h ^ 0x3c6eull};
+        long long i = 0;
+        for (; i + 3 * step < len; i += 4 * step)
+            for (int k = 0; k < 4; ++k)
+                c[k] = mix(c[k], (unsigned)a[i + k * step] + (unsigned long long)(i + k * step) * 31);
+        for (; i < len; i += step) c[0] = mix(c[0], (unsigned)a[i] + (unsigned long long)i * 31);
+        h = mix(mix(mix(mix(h, c[0]), c[1]), c[2]), c[3]);
         h = mix(h, (unsigned)a[len - 1]);
     };
     sample(Acol, (long long)n + 1);
