@@ -42,14 +42,21 @@ extern "C" {
 #define TFLOWS_METHOD_CGS       2 /* Process/CGS.f90                         */
 #define TFLOWS_METHOD_BICG_TRUE 3 /* extension: shadow sequence uses A^T     */
 
-#define TFLOWS_FP64  0 /* reference arithmetic: FP64 throughout              */
+#define TFLOWS_FP64  0 /* reference arithmetic: FP64 throughout, every a*b+c
+                          a rounded product then a rounded sum, the diagonal
+                          preconditioner a division (as the reference)      */
 #define TFLOWS_MIXED 1 /* FP32 inner Krylov solves inside FP64 refinement    */
+#define TFLOWS_FP64_FMA 2 /* FP64 throughout with fused multiply-adds and a
+                          reciprocal diagonal: the reference's recurrences
+                          with about half the FP64 instructions, results
+                          that differ from the reference's by rounding only */
 
 #define TFLOWS_TOL_ABSOLUTE 0 /* stop when ||r||_2 < tol (the reference)    */
 #define TFLOWS_TOL_RELATIVE 1 /* stop when ||r||_2 < tol * ||b||_2           */
 
 typedef struct tflows_options {
-    int precision;       /* TFLOWS_FP64 (default) or TFLOWS_MIXED            */
+    int precision;       /* TFLOWS_FP64 (default), TFLOWS_MIXED or
+                            TFLOWS_FP64_FMA                                 */
     int tol_mode;        /* TFLOWS_TOL_ABSOLUTE (default) or _RELATIVE       */
     double inner_rtol;   /* mixed: FP32 residual reduction between FP64
                             refinements (default 1e-1)                      */

@@ -18,11 +18,11 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libtflows_krylov.so")
-SOURCES = ("krylov.cu", "shim.cu", "noalloc.cu", "tune.cu")
-HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "internal.h")
+SOURCES = ("krylov.cu", "krylov_fma.cu", "shim.cu", "noalloc.cu", "tune.cu")
+HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "solver_entry.cuh", "internal.h")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fno-strict-aliasing", "-Xptxas", "-v" if os.environ.get(
                   "TFLOWS_PTXAS_VERBOSE") else "-O3"]
 
@@ -61,8 +61,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         def compile_one(src):
             obj = os.path.join(BUILD, src.replace(".cu", ".o"))
             extra = os.environ.get("TFLOWS_NVCC_EXTRA", "").split()
-            cmd = [cc, *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-c", os.path.join(CSRC, src),
-                   "-o", obj]
+            # the contracted build fuses multiply-adds; everything else keeps
+            # the reference's separately rounded products and sums
+            fmad = ["--fmad=true"] if src == "krylov_fma.cu" else ["--fmad=false"]
+            cmd = [cc, *ARCH, *NVCC_FLAGS, *fmad, *extra, "-I", INCLUDE, "-c",
+                   os.path.join(CSRC, src), "-o", obj]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise NativeLibraryError(f"nvcc failed for {src}:\n{r.stderr}")

@@ -24,7 +24,7 @@ from . import _native
 OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT, BAD_INPUT, CUDA_ERROR, NO_DEVICE, UNSUPPORTED = \
     range(9)
 CG, BICG, CGS, BICG_TRUE = 0, 1, 2, 3
-FP64, MIXED = 0, 1
+FP64, MIXED, FP64_FMA = 0, 1, 2
 TOL_ABSOLUTE, TOL_RELATIVE = 0, 1
 METHODS = {"cg": CG, "bicg": BICG, "cgs": CGS, "bicg_true": BICG_TRUE}
 

@@ -147,6 +147,14 @@ cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, do
 cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, const double* x,
                               double* g, cudaStream_t s);
 
+// The persistent kernels, built twice: krylov.cu with the reference's
+// arithmetic (separate rounded products and sums, dividing diagonal) and
+// krylov_fma.cu with fused multiply-adds (TFLOWS_FP64_FMA and mixed solves).
+enum class KernelId { Cg, Cgs, BicgTrue, Prec1, MixedRestart, MixedReliable, MixedCgs, BatchFp64,
+                      BatchMixed };
+const void* ref_kernel(KernelId id);
+const void* fma_kernel(KernelId id);
+
 // tune.cu: launch-shape autotuner.
 struct TuneChoice {
     int block = 256;

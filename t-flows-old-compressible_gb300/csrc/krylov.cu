@@ -1,6 +1,9 @@
 // Kernels and launchers of libtflows_krylov.so.
+// Kernels of the reference-arithmetic build (--fmad=false) and the host
+// side of every solve, batched launch and plan.
+#define TFLOWS_KNS ref
 #include "internal.h"
-#include "krylov_kernels.cuh"
+#include "solver_entry.cuh"
 
 #include <cuda_bf16.h>
 
@@ -11,130 +14,6 @@
 namespace tflows {
 
 namespace {
-
-// Threads per block of the persistent kernels unless a launch asks for
-// another multiple of 32 up to kMaxBlock (the tuner's choice).  Register
-// budget: 65536 / (kBlock * kMinBlocks) per thread, i.e. kMinBlocks resident
-// blocks of kBlock threads per SM.
-constexpr int kBlock = 256;
-constexpr int kMaxBlock = 512;
-#ifndef TFLOWS_MINBLOCKS
-#define TFLOWS_MINBLOCKS 4
-#endif
-constexpr int kMinBlocks = TFLOWS_MINBLOCKS;
-constexpr int kMinBlocksAtMax = kMinBlocks * kBlock / kMaxBlock > 0 ? kMinBlocks * kBlock / kMaxBlock : 1;
-
-template <typename T>
-struct KParams {
-    Mat<T> m;
-    Mat<T> mT;  // A^T values in A's pattern (true BiCG only)
-    Vecs<T> v;
-    SolveCfg cfg;
-    DevCtl* ctl;
-    DevState* state;
-    double* partials;
-    long long timeout_cyc;
-    int mode;  // 0 solve, 1 Prec1 only
-    int stall;
-};
-
-__device__ int status_of(const SolveOut& o, const DevCtl* ctl) {
-    if (ctl->status != 0) return ctl->status;
-    switch (o.exit_kind) {
-        case EXIT_MAXITER: return isfinite(o.fin_res) ? ST_NOT_CONVERGED : ST_NONFINITE;
-        case EXIT_NONFINITE: return ST_NONFINITE;
-        case EXIT_ABORT: return ST_TIMEOUT;
-        default: return ST_OK;
-    }
-}
-
-// METHOD: 0 CG (and BiCG), 2 CGS, 9 Prec1 only.
-template <typename T, int METHOD>
-__global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax) krylov_kernel(KParams<T> P) {
-    Grid g;
-    grid_init(g, P.ctl, P.partials, P.timeout_cyc);
-    g.stall = P.stall;
-    SolveOut out;
-    out.exit_kind = 0;
-    out.iterations = 0;
-    out.ini_res = 0.0;
-    out.fin_res = 0.0;
-    out.bnrm2 = 0.0;
-    if (METHOD == 9) {
-        bool ok = prec1_phase(g, P.m, P.v.D, P.cfg.prec);
-        out.exit_kind = ok ? EXIT_CONVERGED : EXIT_ABORT;
-    } else if (METHOD == 2) {
-        cgs_solve(g, P.m, P.v, P.cfg, out);
-    } else if (METHOD == 3) {
-        bicg_true_solve(g, P.m, P.mT, P.v, P.cfg, out);
-    } else {
-        cg_solve(g, P.m, P.v, P.cfg, out);
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        DevState* s = P.state;
-        s->status = status_of(out, P.ctl);
-        s->exit_kind = out.exit_kind;
-        s->iterations = out.iterations;
-        s->inner_iters = 0;
-        s->refinements = 0;
-        s->ini_res = out.ini_res;
-        s->fin_res = out.fin_res;
-        s->bnrm2 = out.bnrm2;
-        s->timeout_where = P.ctl->where;
-    }
-}
-
-struct MixedParams {
-    Mat<double> m64;
-    Mat<float> m32;
-    double* x64;
-    double* r64;
-    const double* b64;
-    double* D64;
-    double* xbest;
-    Vecs<float> v32;
-    MixedCfg cfg;
-    DevCtl* ctl;
-    DevState* state;
-    double* partials;
-    long long timeout_cyc;
-    int stall;
-};
-
-// KIND: 0 restarted CG, 2 restarted CGS, 1 CG with reliable updates.
-template <int KIND>
-__global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax) mixed_kernel(MixedParams P) {
-    Grid g;
-    grid_init(g, P.ctl, P.partials, P.timeout_cyc);
-    g.stall = P.stall;
-    MixedOut out;
-    out.exit_kind = 0;
-    out.iterations = 0;
-    out.refinements = 0;
-    out.ini_res = 0.0;
-    out.fin_res = 0.0;
-    out.bnrm2 = 0.0;
-    if (KIND == 1)
-        mixed_cg_reliable(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.xbest, P.v32, P.cfg,
-                          out);
-    else
-        mixed_solve(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.v32, P.cfg, out);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        DevState* s = P.state;
-        SolveOut o;
-        o.exit_kind = out.exit_kind;
-        o.fin_res = out.fin_res;
-        s->status = status_of(o, P.ctl);
-        s->exit_kind = out.exit_kind;
-        s->iterations = out.iterations;
-        s->inner_iters = out.iterations;
-        s->refinements = out.refinements;
-        s->ini_res = out.ini_res;
-        s->fin_res = out.fin_res;
-        s->bnrm2 = out.bnrm2;
-        s->timeout_where = P.ctl->where;
-    }
-}
 
 template <typename T>
 __global__ void fill_kernel(T* p, long long n, T v) {
@@ -410,7 +289,7 @@ int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, doubl
     P.timeout_cyc = timeout_cycles(timeout_s);
     P.mode = 1;
     cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
-    auto kern = krylov_kernel<double, 9>;
+    const void* kern = ref_kernel(KernelId::Prec1);
     SolveRequest rq;
     const int grid = choose_grid(t, rq, max_coresident(kern, kBlock));
     cudaError_t e = launch_coop(kern, P, grid, kBlock, s);
@@ -574,91 +453,42 @@ int launch_and_report(K kern, P& params, const DeviceTopology& t, Workspace& ws,
     return rep.status;
 }
 
-// ---- batched solves: one cooperative launch, one block group per system ------
-struct BatchItem {
-    int b0;       // first block of the group
-    int nb;       // blocks in the group
-    int mixed;    // 0: FP64 params, 1: mixed params
-    int method;   // 0 CG, 2 CGS
-    KParams<double> P64;
-    MixedParams PM;
-};
+}  // namespace
 
-template <int MIXED>
-__global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax)
-    batch_kernel(const BatchItem* __restrict__ items, const int* __restrict__ block_item) {
-    const BatchItem& it = items[block_item[blockIdx.x]];
-    const unsigned long long t_start = globaltimer_ns();
-    Grid g;
-    if (!MIXED) {
-        KParams<double> P = it.P64;
-        grid_init_group(g, P.ctl, P.partials, P.timeout_cyc, it.b0, it.nb);
-        SolveOut out;
-        out.exit_kind = 0;
-        out.iterations = 0;
-        out.ini_res = 0.0;
-        out.fin_res = 0.0;
-        out.bnrm2 = 0.0;
-        if (it.method == 2) cgs_solve(g, P.m, P.v, P.cfg, out);
-        else cg_solve(g, P.m, P.v, P.cfg, out);
-        if (g.bid == 0 && threadIdx.x == 0) {
-            DevState* s = P.state;
-            s->status = status_of(out, P.ctl);
-            s->exit_kind = out.exit_kind;
-            s->iterations = out.iterations;
-            s->inner_iters = 0;
-            s->refinements = 0;
-            s->ini_res = out.ini_res;
-            s->fin_res = out.fin_res;
-            s->bnrm2 = out.bnrm2;
-            s->timeout_where = P.ctl->where;
-            s->group_ns = (double)(globaltimer_ns() - t_start);
-        }
-    } else {
-        MixedParams P = it.PM;
-        grid_init_group(g, P.ctl, P.partials, P.timeout_cyc, it.b0, it.nb);
-        MixedOut out;
-        out.exit_kind = 0;
-        out.iterations = 0;
-        out.refinements = 0;
-        out.ini_res = 0.0;
-        out.fin_res = 0.0;
-        out.bnrm2 = 0.0;
-        mixed_solve(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.v32, P.cfg, out);
-        if (g.bid == 0 && threadIdx.x == 0) {
-            DevState* s = P.state;
-            SolveOut o;
-            o.exit_kind = out.exit_kind;
-            o.fin_res = out.fin_res;
-            s->status = status_of(o, P.ctl);
-            s->exit_kind = out.exit_kind;
-            s->iterations = out.iterations;
-            s->inner_iters = out.iterations;
-            s->refinements = out.refinements;
-            s->ini_res = out.ini_res;
-            s->fin_res = out.fin_res;
-            s->bnrm2 = out.bnrm2;
-            s->timeout_where = P.ctl->where;
-            s->group_ns = (double)(globaltimer_ns() - t_start);
-        }
+const void* ref_kernel(KernelId id) {
+    switch (id) {
+        case KernelId::Cg: return (const void*)ref::krylov_kernel<double, 0>;
+        case KernelId::Cgs: return (const void*)ref::krylov_kernel<double, 2>;
+        case KernelId::BicgTrue: return (const void*)ref::krylov_kernel<double, 3>;
+        case KernelId::Prec1: return (const void*)ref::krylov_kernel<double, 9>;
+        case KernelId::BatchFp64: return (const void*)ref::batch_kernel<0>;
+        default: return nullptr;  // mixed solves are built with contraction only
     }
+}
+
+namespace {
+
+// The kernel a request runs: reference arithmetic for TFLOWS_FP64, the
+// contracted build for TFLOWS_FP64_FMA and for the mixed solves.
+const void* solver_kernel(const SolveRequest& rq) {
+    if (rq.precision == 1)
+        return fma_kernel(rq.method == 2 ? KernelId::MixedCgs
+                                         : (rq.refine_restart ? KernelId::MixedRestart
+                                                              : KernelId::MixedReliable));
+    const KernelId id = rq.method == 2 ? KernelId::Cgs
+                        : rq.method == 3 ? KernelId::BicgTrue : KernelId::Cg;
+    return rq.precision == 2 ? fma_kernel(id) : ref_kernel(id);
+}
+
+const void* batch_kernel_for(int precision) {
+    return precision == 1 ? fma_kernel(KernelId::BatchMixed)
+           : precision == 2 ? fma_kernel(KernelId::BatchFp64) : ref_kernel(KernelId::BatchFp64);
 }
 
 }  // namespace
 
 int planned_grid(const DeviceTopology& t, const SolveRequest& rq) {
-    const int block = block_of(rq);
-    int maxb;
-    if (rq.precision == 1)
-        maxb = max_coresident(rq.method == 2 ? mixed_kernel<2>
-                                             : (rq.refine_restart ? mixed_kernel<0> : mixed_kernel<1>),
-                              block);
-    else
-        maxb = max_coresident(rq.method == 2   ? krylov_kernel<double, 2>
-                              : rq.method == 3 ? krylov_kernel<double, 3>
-                                               : krylov_kernel<double, 0>,
-                              block);
-    return choose_grid(t, rq, maxb);
+    return choose_grid(t, rq, max_coresident(solver_kernel(rq), block_of(rq)));
 }
 
 int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
@@ -666,16 +496,11 @@ int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, do
     if (rq.precision == 1) {
         MixedParams P;
         cudaError_t e = prepare_mixed(t, ws, rq, x, r, s, P);
-        auto kern = P.cfg.method == 2 ? mixed_kernel<2>
-                                      : (P.cfg.restart ? mixed_kernel<0> : mixed_kernel<1>);
-        return launch_and_report(kern, P, t, ws, rq, s, rep, e);
+        return launch_and_report(solver_kernel(rq), P, t, ws, rq, s, rep, e);
     }
     KParams<double> P;
     cudaError_t e = prepare_fp64(t, ws, rq, x, r, s, P);
-    auto kern = P.cfg.method == 2   ? krylov_kernel<double, 2>
-                : P.cfg.method == 3 ? krylov_kernel<double, 3>
-                                    : krylov_kernel<double, 0>;
-    return launch_and_report(kern, P, t, ws, rq, s, rep, e);
+    return launch_and_report(solver_kernel(rq), P, t, ws, rq, s, rep, e);
 }
 
 // Persistent launch state of a batched solve: pinned host and device copies
@@ -745,21 +570,22 @@ void fail_all(std::vector<BatchSpec>& specs, int status, const std::string& msg)
 
 cudaError_t batch_reserve(BatchLaunch* L, int count, int block) {
     if (block <= 0) block = kBlock;
-    const int maxb = std::max(max_coresident(batch_kernel<0>, block),
-                              max_coresident(batch_kernel<1>, block));
+    int maxb = 1;
+    for (int p : {0, 1, 2}) maxb = std::max(maxb, max_coresident(batch_kernel_for(p), block));
     return grow(*L, count, maxb);
 }
 
 int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s) {
     const int count = (int)specs.size();
     if (count == 0) return ST_OK;
-    const bool mixed = specs[0].rq.precision == 1;
+    const int precision = specs[0].rq.precision;
+    const bool mixed = precision == 1;
     for (auto& sp : specs)
-        if ((sp.rq.precision == 1) != mixed) {
+        if (sp.rq.precision != precision) {
             fail_all(specs, ST_BAD_INPUT, "one precision per batched launch");
             return ST_BAD_INPUT;
         }
-    auto kern = mixed ? batch_kernel<1> : batch_kernel<0>;
+    const void* kern = batch_kernel_for(precision);
     const int block = block_of(specs[0].rq);
     for (auto& sp : specs)
         if (block_of(sp.rq) != block) {
@@ -836,7 +662,8 @@ int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s)
         cfg.numAttrs = 1;
         const BatchItem* di = L->d_items;
         const int* dm = L->d_map;
-        e = cudaLaunchKernelEx(&cfg, kern, di, dm);
+        void* args[] = {(void*)&di, (void*)&dm};
+        e = cudaLaunchKernelExC(&cfg, kern, args);
     }
     for (int k = 0; k < count && e == cudaSuccess; ++k)
         e = cudaMemcpyAsync(L->h_state + k, specs[k].ws->state, sizeof(DevState),

@@ -8,8 +8,9 @@
 // 32 consecutive words.  Each row keeps its entries in the caller's stored
 // order, so every per-row sum runs left to right exactly as the reference's
 // loops do (Process/CG.f90:193-199, Resid.f90:28-33); padding slots carry
-// column -1 and are skipped.  With --fmad=false every a*b+c is a rounded
-// product followed by a rounded sum, as in the reference.
+// column -1 and are skipped.  In the reference-arithmetic build (--fmad=false)
+// every a*b+c is a rounded product followed by a rounded sum, as in the
+// reference; the contracted build fuses them (solver_entry.cuh).
 //
 // One cooperative launch runs a whole solve.  Phases are separated by the
 // bounded grid barrier of device_common.cuh; the three scalar all-reduces
@@ -142,9 +143,16 @@ __device__ __forceinline__ void publish_t(Grid& g, int slot, const T (&v)[K]) {
     publish<K>(g, slot, d);
 }
 
-// Jacobi step z = r / D.  FP64 keeps the reference's correctly rounded
-// division; the FP32 inner solves hold 1/D and multiply.
+// Jacobi step z = r / D.  The reference-arithmetic build keeps the
+// reference's correctly rounded division; the contracted build
+// (TFLOWS_FP64_RECIP_DIAG) and the FP32 inner solves hold 1/D and multiply.
+#ifdef TFLOWS_FP64_RECIP_DIAG
+constexpr bool kRecipDiag64 = true;
+__device__ __forceinline__ double jacobi(double r, double dinv) { return r * dinv; }
+#else
+constexpr bool kRecipDiag64 = false;
 __device__ __forceinline__ double jacobi(double r, double d) { return r / d; }
+#endif
 __device__ __forceinline__ float jacobi(float r, float dinv) { return r * dinv; }
 
 // q_i = sum_j a_ij x_j over row i = 32*s + lane, left to right from 0.  Rows
@@ -362,7 +370,12 @@ __device__ bool prec1_phase(Grid& g, const Mat<T>& m, T* D, int prec) {
         const bool synced = grid_sync(g, 12);
         return ok && synced;
     }
-    TF_FOR_ROWS(g, m, i) { D[i] = (prec == 1) ? diag_value(m, i) : T(1); }
+    // with a reciprocal diagonal (contracted FP64 build) D holds 1 / a_ii
+    TF_FOR_ROWS(g, m, i) {
+        D[i] = (prec == 1) ? (sizeof(T) == 8 && kRecipDiag64 ? T(1) / diag_value(m, i)
+                                                            : diag_value(m, i))
+                           : T(1);
+    }
     return true;  // made visible by the caller's next barrier
 }
 
@@ -998,7 +1011,7 @@ __device__ __forceinline__ bool mixed_residual(Grid& g, const Mat<double>& m64, 
     return true;
 }
 
-__device__ void mixed_solve(Grid& g, const Mat<double>& m64, const Mat<float>& m32, double* x64,
+static __device__ void mixed_solve(Grid& g, const Mat<double>& m64, const Mat<float>& m32, double* x64,
                             double* r64, const double* b64, double* D64, Vecs<float>& v32,
                             const MixedCfg& c, MixedOut& out) {
     out.exit_kind = EXIT_ABORT;
@@ -1013,7 +1026,8 @@ __device__ void mixed_solve(Grid& g, const Mat<double>& m64, const Mat<float>& m
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             // FP32 solves hold 1/D for the diagonal preconditioner
-            df.a[u] = c.prec == 1 ? (float)(1.0 / d.a[u]) : (float)d.a[u];
+            df.a[u] = c.prec == 1 ? (float)(kRecipDiag64 ? d.a[u] : 1.0 / d.a[u])
+                                  : (float)d.a[u];
             wf.a[u] = Cell<float>::sentinel();
             if (i + u < m64.n) acc[0] += bb.a[u] * bb.a[u];
         }
@@ -1121,7 +1135,7 @@ __device__ void mixed_solve(Grid& g, const Mat<double>& m64, const Mat<float>& m
 // values, the convergence test ||r|| < tol is made on it in FP64, and the
 // FP32 residual is replaced by it.  Unlike a restarted refinement the search
 // direction is kept, so the iteration count stays close to the FP64 solve's.
-__device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const Mat<float>& m32,
+static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const Mat<float>& m32,
                                   double* x64, double* r64, const double* b64, double* D64,
                                   double* xbest, Vecs<float>& v, const MixedCfg& c,
                                   MixedOut& out) {
@@ -1136,7 +1150,8 @@ __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const Mat<flo
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             // FP32 solves hold 1/D for the diagonal preconditioner
-            df.a[u] = c.prec == 1 ? (float)(1.0 / d.a[u]) : (float)d.a[u];
+            df.a[u] = c.prec == 1 ? (float)(kRecipDiag64 ? d.a[u] : 1.0 / d.a[u])
+                                  : (float)d.a[u];
             wf.a[u] = Cell<float>::sentinel();
             if (i + u < m64.n) acc[0] += bb.a[u] * bb.a[u];
         }

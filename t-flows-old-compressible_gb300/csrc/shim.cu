@@ -385,6 +385,11 @@ SolveRequest make_request(const tflows_options& o, int method, int prec, int max
 
 // Launch-shape options a kernel launch can take.
 bool shape_ok(const SolveRequest& rq, std::string& msg) {
+    if (rq.precision != TFLOWS_FP64 && rq.precision != TFLOWS_MIXED &&
+        rq.precision != TFLOWS_FP64_FMA) {
+        msg = "precision must be TFLOWS_FP64, TFLOWS_MIXED or TFLOWS_FP64_FMA";
+        return false;
+    }
     if (rq.block != 0 && (rq.block % 32 != 0 || rq.block < 64 || rq.block > 512)) {
         msg = "block_size must be 0 or a multiple of 32 in 64..512";
         return false;
@@ -449,8 +454,8 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
     SolveRequest rq = rq0;
     if (std::string msg; !shape_ok(rq, msg)) return fail(TFLOWS_BAD_INPUT, msg);
     if (rq.method == TFLOWS_METHOD_BICG_TRUE) {
-        if (rq.precision != TFLOWS_FP64)
-            return fail(TFLOWS_UNSUPPORTED, "true BiCG runs in FP64 only");
+        if (rq.precision == TFLOWS_MIXED)
+            return fail(TFLOWS_UNSUPPORTED, "true BiCG runs in FP64 only (TFLOWS_FP64 or _FP64_FMA)");
         if (rq.prec == 2) return fail(TFLOWS_UNSUPPORTED, "true BiCG takes prec 0 or 1");
         if (cudaError_t e = build_transpose(tp->t); e != cudaSuccess)
             return cuda_fail(e, "transpose map");
@@ -468,7 +473,7 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
     cudaError_t e = ensure_workspace(tp->ws, tp->t);
     if (e == cudaSuccess && rq.ic_bf16) e = ensure_lu16(tp->ws);
     if (e != cudaSuccess) return cuda_fail(e, "workspace");
-    if ((e = permute_values(tp->t, tp->ws, d_val, true, rq.precision != TFLOWS_FP64, s,
+    if ((e = permute_values(tp->t, tp->ws, d_val, true, rq.precision == TFLOWS_MIXED, s,
                             rq.ic_bf16 != 0)) != cudaSuccess)
         return cuda_fail(e, "value layout");
     if (rq.method == TFLOWS_METHOD_BICG_TRUE &&
@@ -848,7 +853,7 @@ int tflows_solve_batched_device(int count, tflows_topology* const* topos, const 
         cudaError_t e = ensure_workspace(*ws, tp->t);
         if (e == cudaSuccess && rq.ic_bf16) e = ensure_lu16(*ws);
         if (e == cudaSuccess)
-            e = permute_values(tp->t, *ws, vals[k], true, rq.precision != TFLOWS_FP64, s,
+            e = permute_values(tp->t, *ws, vals[k], true, rq.precision == TFLOWS_MIXED, s,
                                rq.ic_bf16 != 0);
         double* X = ws->vec64 + 11 * ws->vec_cap;
         double* R = ws->vec64 + 12 * ws->vec_cap;
@@ -944,7 +949,7 @@ int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* top
         cudaStream_t ts = plan->cap;
         for (int k = 0; k < count && e == cudaSuccess; ++k) {
             BatchSpec& sp = plan->specs[k];
-            e = permute_values(*sp.t, *sp.ws, vals[k], true, sp.rq.precision != TFLOWS_FP64, ts,
+            e = permute_values(*sp.t, *sp.ws, vals[k], true, sp.rq.precision == TFLOWS_MIXED, ts,
                                sp.rq.ic_bf16 != 0);
         }
         if (e != cudaSuccess) return cuda_fail(e, "plan tuning");
@@ -976,7 +981,7 @@ int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* top
     for (int k = 0; k < count && e == cudaSuccess; ++k) {
         BatchSpec& sp = plan->specs[k];
         const size_t nb = sizeof(double) * sp.t->n;
-        e = permute_values(*sp.t, *sp.ws, vals[k], true, sp.rq.precision != TFLOWS_FP64, s,
+        e = permute_values(*sp.t, *sp.ws, vals[k], true, sp.rq.precision == TFLOWS_MIXED, s,
                            sp.rq.ic_bf16 != 0);
         if (e == cudaSuccess) e = cudaMemcpyAsync(sp.x, xs[k], nb, cudaMemcpyDeviceToDevice, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(sp.r, bs[k], nb, cudaMemcpyDeviceToDevice, s);
@@ -1064,7 +1069,7 @@ int tflows_autotune(tflows_topology* topo, int method, int prec, const tflows_op
     cudaError_t e = ensure_workspace(topo->ws, topo->t);
     if (e == cudaSuccess && rq.ic_bf16) e = ensure_lu16(topo->ws);
     if (e == cudaSuccess)
-        e = permute_values(topo->t, topo->ws, val, true, rq.precision != TFLOWS_FP64, s,
+        e = permute_values(topo->t, topo->ws, val, true, rq.precision == TFLOWS_MIXED, s,
                            rq.ic_bf16 != 0);
     if (e != cudaSuccess) return cuda_fail(e, "tuning setup");
     TuneChoice ch;

@@ -81,7 +81,7 @@ def test_golden_prec1_resid_bitwise(path):
     assert np.array_equal(r.view(np.uint64), g["resid_r1_out"].view(np.uint64))
 
 
-def _oracle_vs_gpu(s, method, prec, rel_tol, niter=2000, x0=None, it_slack=1):
+def _oracle_vs_gpu(s, method, prec, rel_tol, niter=2000, x0=None, it_slack=1, opts=None):
     tol = rel_tol * float(np.linalg.norm(s.b))
     x_in = s.x.copy() if x0 is None else x0
     xo, ro, ito, inio, fino = oracle.solve(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia,
@@ -89,7 +89,7 @@ def _oracle_vs_gpu(s, method, prec, rel_tol, niter=2000, x0=None, it_slack=1):
     xg = x_in.copy()
     rg = s.b.copy()
     out = tflows.solve_ex(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab, xg, rg,
-                          prec, niter, tol)
+                          prec, niter, tol, opts=opts)
     assert abs(out.niter - ito) <= it_slack, (out.niter, ito)
     assert rel_diff(xg, xo) <= REL, rel_diff(xg, xo)
     assert abs(out.IniRes - inio) <= 1e-11 * inio
@@ -229,3 +229,106 @@ def test_true_bicg_extension_converges_where_cg_recurrence_fails():
     with pytest.raises(tflows.SolverError):
         tflows.solve_ex("bicg_true", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
                         s.x.copy(), s.b.copy(), 2, 100, tol)
+
+
+# ---- TFLOWS_FP64_FMA: the same recurrences with fused multiply-adds and a
+# reciprocal diagonal; every result within the FP64 bar of the reference's.
+
+def _fma():
+    return tflows.options(precision=tflows.FP64_FMA)
+
+
+@pytest.mark.parametrize("path", SOLVER_CASES, ids=lambda p: os.path.basename(p)[:-4])
+def test_fp64_fma_golden_solver_cases(path):
+    g = np.load(path)
+    opts = _fma()
+    for c in range(int(g["ncalls"])):
+        p = f"c{c}_"
+        x = g[p + "x_in"].copy()
+        r = g[p + "r1_in"].copy()
+        out = tflows.solve_ex(str(g[p + "method"]), int(g["N"]), int(g["NB"]), int(g["NONZ"]),
+                              g["A"], g["Acol"], g["Arow"], g["Adia"], g["Ab"], x, r,
+                              int(g[p + "prec"]), int(g[p + "niter_in"]), float(g[p + "tol"]),
+                              float(g[p + "IniRes_in"]), float(g[p + "FinRes_in"]), opts=opts)
+        assert abs(out.niter - int(g[p + "niter_out"])) <= 1, (c, out)
+        xg, rg = g[p + "x_out"], g[p + "r1_out"]
+        assert np.array_equal(np.isnan(x), np.isnan(xg))
+        if np.isnan(rg).any():
+            assert np.isnan(out.FinRes)
+            continue
+        assert rel_diff(x, xg) <= REL, (c, rel_diff(x, xg))
+        ini_g = float(g[p + "IniRes_out"])
+        assert abs(out.IniRes - ini_g) <= 1e-12 * max(abs(ini_g), 1e-300)
+
+
+def test_fp64_fma_config1():
+    out, _ = _oracle_vs_gpu(mesh.config_system(1), "cg", 1, 1e-12, opts=_fma())
+    assert out.status == tflows.OK
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_fp64_fma_pressure_vd_cg(prec):
+    s = mesh.pressure_system(20, 18, 16, perturb=0.2, seed=11, variable_density=True)
+    _oracle_vs_gpu(s, "cg", prec, 1e-12, niter=4000, it_slack=2, opts=_fma())
+
+
+@pytest.mark.parametrize("method,prec", [("bicg", 1), ("bicg", 2), ("cgs", 0), ("cgs", 1),
+                                         ("cgs", 2)])
+def test_fp64_fma_convection_diffusion(method, prec):
+    s = mesh.convection_diffusion_system(24, 20, 18, perturb=0.2, seed=5)
+    _oracle_vs_gpu(s, method, prec, 1e-12, it_slack=2, opts=_fma())
+
+
+def test_fp64_fma_full_size_config2():
+    """The 128^3 benchmark system: the same iteration counts as the
+    reference arithmetic and solutions within the FP64 bar of each other."""
+    s = mesh.config_system(2)
+    for method in ("bicg", "cgs"):
+        xs, its = {}, {}
+        for name, opts in (("ref", tflows.options()), ("fma", _fma())):
+            x, r = s.x.copy(), s.b.copy()
+            out = tflows.solve_ex(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
+                                  x, r, 1, 200, s.tol, opts=opts)
+            assert out.status == tflows.OK and out.FinRes < s.tol
+            xs[name], its[name] = x, out.niter
+        assert abs(its["ref"] - its["fma"]) <= 1, its
+        assert rel_diff(xs["fma"], xs["ref"]) <= REL
+        true_r = s.b - s.scipy() @ xs["fma"][s.NB + 1:]
+        assert np.linalg.norm(true_r) < 2 * s.tol
+
+
+def test_fp64_fma_true_bicg_and_batched():
+    import torch
+    s = mesh.convection_diffusion_system(14, 12, 10, perturb=0.2, seed=5, dt=1.0)
+    tol = 1e-10 * float(np.linalg.norm(s.b))
+    x, r = s.x.copy(), s.b.copy()
+    out = tflows.solve_ex("bicg_true", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
+                          x, r, 1, 2000, tol, opts=_fma())
+    assert out.status == tflows.OK
+    assert np.linalg.norm(s.b - s.scipy() @ x[s.NB + 1:]) < 2 * tol
+    p = mesh.pressure_system(12, 11, 10, perturb=0.2, seed=2, variable_density=True)
+    systems = [(p, "cg", 2), (s, "cgs", 1)]
+    topos = [tflows.Topology.from_system(m) for m, _, _ in systems]
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+    vals = [dev(m.A[:-1]) for m, _, _ in systems]
+    bs = [dev(m.b) for m, _, _ in systems]
+    xs = [torch.zeros(m.N, dtype=torch.float64, device="cuda") for m, _, _ in systems]
+    tols = [1e-10 * float(np.linalg.norm(m.b)) for m, _, _ in systems]
+    res = tflows.solve_batched(topos, vals, bs, xs, [k for _, k, _ in systems],
+                               [q for _, _, q in systems], [3000, 3000], tols, _fma())
+    for k, (m, _, _) in enumerate(systems):
+        assert res[k]["status"] == tflows.OK, res[k]
+        assert np.linalg.norm(m.b - m.scipy() @ xs[k].cpu().numpy()) < 2 * tols[k]
+    for t in topos:
+        t.close()
+
+
+def test_bad_precision_rejected():
+    s = mesh.pressure_system(6, 6, 6, seed=1)
+    with pytest.raises(tflows.SolverError) as e:
+        tflows.solve_ex("cg", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab, s.x.copy(),
+                        s.b.copy(), 1, 100, 1e-8, opts=tflows.options(precision=7))
+    assert e.value.status == tflows.BAD_INPUT
