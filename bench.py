@@ -249,6 +249,7 @@ def mixed_vs_fp64(pkg, dev, scale, precs, reps):
     result = {}
     for prec in precs:
         fp, x64 = run(prec, pkg.options(precision=pkg.FP64))
+        fpf, _ = run(prec, pkg.options(precision=pkg.FP64_FMA))
         variants = IC_VARIANTS if prec == 2 else (("jacobi_fp32", {}),)
         mixed = {}
         for label, kw in variants:
@@ -258,8 +259,10 @@ def mixed_vs_fp64(pkg, dev, scale, precs, reps):
         ok = [k for k in mixed if mixed[k]["status"] == pkg.OK] or list(mixed)
         best = min(ok, key=lambda k: mixed[k]["ms"])
         result[prec] = {"workload": f"{s.name}, CG prec {prec}, tol 1e-8*||b|| absolute",
-                        "n": s.N, "fp64": fp, "mixed": mixed[best], "mixed_variant": best,
+                        "n": s.N, "fp64": fp, "fp64_fma": fpf, "mixed": mixed[best],
+                        "mixed_variant": best,
                         "speedup": fp["ms"] / mixed[best]["ms"],
+                        "speedup_vs_fp64_fma": fpf["ms"] / mixed[best]["ms"],
                         "mixed_rel_diff_vs_fp64": mixed[best]["rel_diff_vs_fp64"]}
         if len(mixed) > 1:
             result[prec]["all_mixed_variants"] = mixed
@@ -319,21 +322,27 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
 
 
 def cfg2_methods(pkg, dev, topo, s, val, b, reps=3):
-    """The other config-2 solvers on the same 128^3 system: CGS (FP64), the
-    true-BiCG extension (shadow sequence with A^T, FP64) and BiCG in mixed
-    precision, each to the same absolute tolerance from x0 = 0."""
+    """The config-2 solvers on the same 128^3 system besides the headline:
+    BiCG and CGS in reference arithmetic (TFLOWS_FP64) and with fused
+    multiply-adds (TFLOWS_FP64_FMA), the true-BiCG extension (shadow sequence
+    with A^T) and BiCG in mixed precision, each to the same absolute
+    tolerance from x0 = 0."""
     import torch
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
     out = {}
-    for label, method, precision in (("cgs_fp64", "cgs", pkg.FP64),
-                                     ("bicg_true_fp64", "bicg_true", pkg.FP64),
+    for label, method, precision in (("bicg_fp64", "bicg", pkg.FP64),
+                                     ("bicg_fp64_fma", "bicg", pkg.FP64_FMA),
+                                     ("cgs_fp64", "cgs", pkg.FP64),
+                                     ("cgs_fp64_fma", "cgs", pkg.FP64_FMA),
+                                     ("bicg_true_fp64_fma", "bicg_true", pkg.FP64_FMA),
                                      ("bicg_mixed", "bicg", pkg.MIXED)):
-        opts = pkg.options(precision=precision)
+        opts = pkg.options(precision=precision, autotune=1)
         el, res = device_solves(pkg, topo, val, b, x, method, 1, s.tol, opts, reps, 1)
         r = res[-1]
         out[label] = {"ms": 1e3 * el / reps, "solves_per_s": reps / el,
                       "iterations": r["iterations"], "status": r["status"],
-                      "gbs": r["bytes"] / r["seconds"] / 1e9, "fin_res": r["fin_res"]}
+                      "gbs": r["bytes"] / r["seconds"] / 1e9, "fin_res": r["fin_res"],
+                      "block_size": r["block_size"], "grid_blocks": r["grid_blocks"]}
     return out
 
 
@@ -458,7 +467,9 @@ def main():
     ap.add_argument("--scale", type=int, default=None, help="box edge (default: the config's)")
     ap.add_argument("--method", default="bicg")
     ap.add_argument("--prec", type=int, default=1)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64_fma", choices=["fp64", "fp64_fma", "mixed"],
+                    help="fp64: reference arithmetic; fp64_fma: FP64 with fused multiply-adds "
+                         "(within 1e-8 of the reference); mixed: FP32 inner + FP64 refinement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--compare-scale", type=int, default=256,
@@ -498,7 +509,7 @@ def main():
     val = torch.from_numpy(s.A[:-1].copy()).to(dev)
     b = torch.from_numpy(s.b.copy()).to(dev)
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
-    prec_mode = pkg.MIXED if args.precision == "mixed" else pkg.FP64
+    prec_mode = {"fp64": pkg.FP64, "fp64_fma": pkg.FP64_FMA, "mixed": pkg.MIXED}[args.precision]
     opts = pkg.options(precision=prec_mode, autotune=int(not args.no_autotune))
     tuning = None
     if not args.no_autotune:
@@ -528,7 +539,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64",
         "data": "synthetic",
         "config": dict(workload_config(s, method, prec, args.precision),
                        launch=({"autotuned": True, **tuning} if tuning else
@@ -537,12 +548,15 @@ def main():
         "time_to_tol_ms": 1e3 * el / args.steps,
     }
     achieved = kern_b / kern_s / 1e9
-    kname = "mixed_kernel" if args.precision == "mixed" else "krylov_kernel_fp64"
+    kname = {"fp64": "krylov_kernel_fp64", "fp64_fma": "krylov_kernel_fp64_fma",
+             "mixed": "mixed_kernel"}[args.precision]
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak,
                         "traffic": profiled_traffic(kname, s.name, method, prec),
-                        "kernel": ("mixed_kernel" if args.precision == "mixed" else
-                                   "krylov_kernel<double>") + " (one persistent launch per solve)",
+                        "kernel": {"fp64": "ref::krylov_kernel<double>",
+                                   "fp64_fma": "fma::krylov_kernel<double>",
+                                   "mixed": "fma::mixed_kernel"}[args.precision]
+                                  + " (one persistent launch per solve)",
                         "peak_kind": peak_kind}
 
     if not args.no_e2e:

@@ -258,7 +258,11 @@ def test_fp64_fma_golden_solver_cases(path):
             continue
         assert rel_diff(x, xg) <= REL, (c, rel_diff(x, xg))
         ini_g = float(g[p + "IniRes_out"])
-        assert abs(out.IniRes - ini_g) <= 1e-12 * max(abs(ini_g), 1e-300)
+        # ||b - A x0|| differs by the rounding of the contracted products,
+        # which scales with ||b|| (a warm start at the solution leaves only
+        # rounding noise in IniRes)
+        bnorm = float(np.linalg.norm(g[p + "r1_in"]))
+        assert abs(out.IniRes - ini_g) <= 1e-12 * max(abs(ini_g), 1e-300) + 1e-13 * bnorm
 
 
 def test_fp64_fma_config1():
