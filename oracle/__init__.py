@@ -25,8 +25,9 @@ _I = ctypes.POINTER(ctypes.c_int)
 
 def build(force: bool = False) -> str:
     """Compile the oracle with make (gcc, -O3 -ffp-contract=off)."""
-    if force or not os.path.exists(LIB_PATH) or (
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "krylov_oracle.c"))):
+    srcs = ("krylov_oracle.c", "assembly_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or any(
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, f)) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -54,6 +55,9 @@ def lib():
             L.oracle_reset_state.restype = None
             L.oracle_error_state.argtypes = []
             L.oracle_error_state.restype = ctypes.c_double
+            L.oracle_calcps_assembly.argtypes = (
+                [ctypes.c_int] * 5 + [ctypes.c_double] + [_I] * 4 + [_D] * 24)
+            L.oracle_calcps_assembly.restype = None
             _lib = L
     return _lib
 
@@ -135,3 +139,29 @@ def topolm(NC, side_c):
                                _ip(sid))
     assert nonz == nnz + 1
     return Acol, Arow, Adia, sid
+
+
+CELL_FIELDS = ("volume", "Asave", "rho_n", "rho_o", "rho_oo", "U", "V", "W", "P", "Px", "Py",
+               "Pz")
+FACE_GEOM = ("Sx", "Sy", "Sz", "Dx", "Dy", "Dz", "f")
+
+
+def calcps_assembly(NC, NbC, NS, NONZ, Nmat, dt, SideC, SidAij, Adia, TypeBC, geom, fields):
+    """Process/CalcPS.f90:49-202 restated (assembly_oracle.c).
+
+    SideC: (NS, 3) int array = SideC(0:2, NS) in memory order; SidAij (NS, 2);
+    Adia (NC,) 1-based; TypeBC and every entry of ``fields`` (CELL_FIELDS)
+    span cells -NbC..NC (index c + NbC); ``geom`` holds the FACE_GEOM arrays.
+    Returns (Aval[NONZ], b[NC], Abou[NbC] (cells -NbC..-1), Flux[NS], errmax).
+    """
+    Aval, b = np.zeros(NONZ), np.zeros(NC)
+    Abou, Flux = np.zeros(max(NbC, 1)), np.zeros(NS)
+    em = ctypes.c_double()
+    keep = [_i32(SideC), _i32(SidAij), _i32(Adia), _i32(TypeBC)]
+    g = [_f64(geom[k]) for k in FACE_GEOM]
+    fl = [_f64(fields[k]) for k in CELL_FIELDS]
+    lib().oracle_calcps_assembly(int(NC), int(NbC), int(NS), int(NONZ), int(Nmat), float(dt),
+                                 *[_ip(a) for a in keep], *[_dp(a) for a in g],
+                                 *[_dp(a) for a in fl], _dp(Aval), _dp(b), _dp(Abou), _dp(Flux),
+                                 ctypes.byref(em))
+    return Aval, b, Abou[:NbC], Flux, em.value

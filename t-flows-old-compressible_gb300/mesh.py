@@ -32,7 +32,7 @@ import numpy as np
 __all__ = [
     "System", "box_csr", "box_geometry", "pressure_system",
     "convection_diffusion_system", "config_system", "batch_sizes",
-    "side_c", "interior_faces", "structured_levels",
+    "side_c", "interior_faces", "structured_levels", "box_faces",
 ]
 
 
@@ -339,6 +339,71 @@ def side_c(nx, ny, nz):
     sid[:ni, 0] = p12 + 1
     sid[:ni, 1] = p21 + 1
     return sc, (Acol, Arow, Adia, sid)
+
+
+def box_faces(nx, ny, nz, perturb=0.0, seed=0):
+    """Every face of a (perturbed) hex box with the geometry the reference
+    keeps per face and cell (Library/GeoLoa.f90: Sx..Sz, Dx..Dz, f, volume),
+    in SideC order: interior x-, y-, z-faces in cell order (as
+    ``interior_faces``), then the six walls (x-min, x-max, y-min, y-max,
+    z-min, z-max, each in cell order) whose second cell is the boundary cell
+    -1, -2, ...  Area vectors point from c1 to c2 (outward on walls);
+    D = centre(c2) - centre(c1), a boundary cell sitting at its face centre;
+    f is the weight of c1 in face interpolation (distance based, 0 on walls).
+
+    Returns a dict: NC, NbC, NS, SideC (NS, 3) = SideC(0:2, NS) in memory
+    order (SideC(0, s) = 0), SidAij (NS, 2), Acol, Arow, Adia (TopolM layout),
+    geometry arrays Sx..Dz and f (NS,), volume (NbC + NC + 1,) over cells
+    -NbC..NC (boundary cells get volume 0), centres xc/yc/zc likewise.
+    """
+    rng = np.random.default_rng(seed)
+    geo = box_geometry(nx, ny, nz, perturb=perturb, rng=rng)
+    sc, (Acol, Arow, Adia, sid) = side_c(nx, ny, nz)
+    C, V = geo["C"], geo["V"]
+    cx, cy, cz = (a.ravel() for a in (C.x, C.y, C.z))
+    S_parts, F_parts = [], []
+    for axis, Sk, Fk in ((0, geo["Sx"], geo["Fx"]), (1, geo["Sy"], geo["Fy"]),
+                         (2, geo["Sz"], geo["Fz"])):
+        sl = (slice(None), slice(None), slice(1, -1)) if axis == 0 else \
+             (slice(None), slice(1, -1), slice(None)) if axis == 1 else \
+             (slice(1, -1), slice(None), slice(None))
+        S_parts.append([a[sl].ravel() for a in (Sk.x, Sk.y, Sk.z)])
+        F_parts.append([a[sl].ravel() for a in (Fk.x, Fk.y, Fk.z)])
+    for axis, Sk, Fk in ((0, geo["Sx"], geo["Fx"]), (1, geo["Sy"], geo["Fy"]),
+                         (2, geo["Sz"], geo["Fz"])):
+        for side, sign in ((0, -1.0), (-1, 1.0)):
+            sl = [slice(None)] * 3
+            sl[2 - axis] = side
+            sl = tuple(sl)
+            S_parts.append([sign * a[sl].ravel() for a in (Sk.x, Sk.y, Sk.z)])
+            F_parts.append([a[sl].ravel() for a in (Fk.x, Fk.y, Fk.z)])
+    S = [np.concatenate([p[k] for p in S_parts]) for k in range(3)]
+    F = [np.concatenate([p[k] for p in F_parts]) for k in range(3)]
+    NS = sc.shape[0]
+    NC = nx * ny * nz
+    c1 = sc[:, 0].astype(np.int64) - 1
+    c2 = sc[:, 1].astype(np.int64)
+    inner = c2 > 0
+    NbC = int(-c2.min()) if (~inner).any() else 0
+    x1 = [cx[c1], cy[c1], cz[c1]]
+    x2 = [np.where(inner, c[np.maximum(c2 - 1, 0)], Fk) for c, Fk in zip((cx, cy, cz), F)]
+    D = [b - a for a, b in zip(x1, x2)]
+    d1 = np.sqrt(sum((Fk - a) ** 2 for Fk, a in zip(F, x1)))
+    d2 = np.sqrt(sum((Fk - b) ** 2 for Fk, b in zip(F, x2)))
+    f = np.where(inner, d2 / (d1 + d2), 0.0)
+    vol = np.zeros(NbC + NC + 1)
+    vol[NbC + 1:] = V.ravel()
+    cen = []
+    for k, c in enumerate((cx, cy, cz)):
+        a = np.zeros(NbC + NC + 1)
+        a[NbC + 1:] = c
+        a[NbC + c2[~inner]] = F[k][~inner]
+        cen.append(a)
+    SideC = np.zeros((NS, 3), np.int32)
+    SideC[:, 1:] = sc
+    return dict(NC=NC, NbC=NbC, NS=NS, SideC=SideC, SidAij=sid, Acol=Acol, Arow=Arow, Adia=Adia,
+                Sx=S[0], Sy=S[1], Sz=S[2], Dx=D[0], Dy=D[1], Dz=D[2], f=f, volume=vol,
+                xc=cen[0], yc=cen[1], zc=cen[2])
 
 
 def _smooth_field(shape, sigma, rng):

@@ -67,7 +67,7 @@ _TOKEN = re.compile(
     r"\s*(?:(?P<num>(?:\d+\.\d*|\.\d+|\d+)(?:[eEdD][+-]?\d+)?)"
     r"|(?P<dotop>\.(?:and|or|not|lt|le|gt|ge|eq|ne|true|false)\.)"
     r"|(?P<name>[a-z_][a-z0-9_]*)"
-    r"|(?P<op>\*\*|<=|>=|==|/=|[-+*/(),<>:]))"
+    r"|(?P<op>\*\*|<=|>=|==|/=|[-+*/(),<>:=]))"
 )
 
 _DOTOPS = {
