@@ -260,6 +260,48 @@ int tflows_spmv_device(tflows_topology *topo, const double *val,
                        const double *x, double *y, int repeat, int fp32,
                        void *stream, double *sec);
 
+/* ---- pressure-correction assembly on the GPU ------------------------------ */
+/* Mesh data of the assembly, resident on the device (host arrays in, copied):
+ * SideC(0:2,NS) and SidAij(2,NS) as the reference holds them (column-major),
+ * Adia(NC) 1-based, TypeBC(-NbC:NC) and volume(-NbC:NC) passed at their
+ * element -NbC, face geometry Sx..Sz, Dx..Dz, f(1:NS) (Library/GeoLoa.f90).
+ * Every index is checked here; bad ones give TFLOWS_BAD_INPUT. */
+typedef struct tflows_assembly tflows_assembly;
+int tflows_assembly_create(tflows_assembly **out, int NC, int NbC, int NS,
+                           int NONZ, const int *SideC, const int *SidAij,
+                           const int *Adia, const int *TypeBC,
+                           const double *Sx, const double *Sy, const double *Sz,
+                           const double *Dx, const double *Dy, const double *Dz,
+                           const double *f, const double *volume, int device);
+void tflows_assembly_destroy(tflows_assembly *a);
+
+/* Per-call cell fields of the assembly: device arrays over cells -NbC..NC,
+ * each passed at its element -NbC (Rho % n, Rho % o, Rho % oo, U/V/W % n,
+ * P % n, the pressure gradient Px/Py/Pz and the momentum diagonal Asave). */
+typedef struct tflows_calcps_fields {
+    const double *rho_n, *rho_o, *rho_oo;
+    const double *u, *v, *w;
+    const double *p, *px, *py, *pz;
+    const double *asave;
+} tflows_calcps_fields;
+
+/* Replaces the assembly part of SUBROUTINE CalcPS (Process/CalcPS.f90:49-202):
+ * Aval(1:NONZ) <- the pressure-correction matrix (zero where no face
+ * writes), Abou(-NbC:-1) <- -A12 on BUFFER faces (passed at -NbC, other
+ * entries untouched), Flux(1:NS) <- the face mass fluxes, b(1:NC) <- the
+ * right-hand side with the density-derivative source and its volume-weighted
+ * mean removed; *errmax (host, may be NULL) <- max |b| before the source.
+ * Device arrays; asynchronous on `stream` unless errmax or seconds is
+ * requested.  Aval, Abou, Flux and errmax are bit-identical to the
+ * reference's sequential loop; b differs from it only by the rounding of
+ * the mean (a tree reduction instead of a left-to-right sum).  *seconds (may
+ * be NULL) <- device time. */
+int tflows_calcps_assemble_device(tflows_assembly *a, int Nmat, double dt,
+                                  const tflows_calcps_fields *fields,
+                                  double *aval, double *b, double *abou,
+                                  double *flux, double *errmax, void *stream,
+                                  double *seconds);
+
 /* ---- allocation-free solve ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that may not allocate GPU
  * memory while they run (device memory reserved up front by another

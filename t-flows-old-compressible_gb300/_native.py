@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libtflows_krylov.so")
-SOURCES = ("krylov.cu", "krylov_fma.cu", "shim.cu", "noalloc.cu", "tune.cu")
+SOURCES = ("krylov.cu", "krylov_fma.cu", "shim.cu", "noalloc.cu", "tune.cu", "assembly.cu")
 HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "solver_entry.cuh", "internal.h")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -132,6 +132,11 @@ class BatchTuning(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class CalcpsFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("rho_n", "rho_o", "rho_oo", "u", "v", "w", "p",
+                                                 "px", "py", "pz", "asave")]
+
+
 _SOLVER = [_I, _I, _I, _D, _I, _I, _I, _D, _D, _D, _I, _I, _D, _D, _D]
 
 SIGNATURES = {
@@ -170,6 +175,13 @@ SIGNATURES = {
     "tflows_autotune": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Options), _VP, _VP, _VP,
                          ctypes.POINTER(Tuning)], ctypes.c_int),
     "tflows_autotune_clear": ([], None),
+    "tflows_assembly_create": ([ctypes.POINTER(_VP), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int] + [_VP] * 12 + [ctypes.c_int], ctypes.c_int),
+    "tflows_assembly_destroy": ([_VP], None),
+    "tflows_calcps_assemble_device": ([_VP, ctypes.c_int, ctypes.c_double,
+                                       ctypes.POINTER(CalcpsFields), _VP, _VP, _VP, _VP,
+                                       ctypes.POINTER(ctypes.c_double), _VP,
+                                       ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "tflows_cg_noalloc": ([ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
                            ctypes.c_int, ctypes.c_double, _VP, _I, _D, _D], ctypes.c_int),
 }

@@ -384,3 +384,61 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+class Assembly:
+    """The pressure-correction assembly of Process/CalcPS.f90:49-202 on the
+    GPU (tflows_assembly_create / tflows_calcps_assemble_device).
+
+    Mesh arrays as the reference holds them: SideC (NS, 3) = SideC(0:2, NS),
+    SidAij (NS, 2), Adia 1-based, TypeBC and volume over cells -NbC..NC,
+    face geometry Sx, Sy, Sz, Dx, Dy, Dz, f.  ``mesh.box_faces`` builds them
+    for a box."""
+
+    GEOM = ("Sx", "Sy", "Sz", "Dx", "Dy", "Dz", "f")
+    FIELDS = ("rho_n", "rho_o", "rho_oo", "u", "v", "w", "p", "px", "py", "pz", "asave")
+
+    def __init__(self, NC, NbC, NS, NONZ, SideC, SidAij, Adia, TypeBC, geom, volume, device=-1):
+        self.NC, self.NbC, self.NS, self.NONZ = int(NC), int(NbC), int(NS), int(NONZ)
+        ints = [np.ascontiguousarray(a, dtype=np.int32) for a in (SideC, SidAij, Adia, TypeBC)]
+        dbls = [np.ascontiguousarray(geom[k], dtype=np.float64) for k in self.GEOM]
+        dbls.append(np.ascontiguousarray(volume, dtype=np.float64))
+        self._h = ctypes.c_void_p()
+        st = lib().tflows_assembly_create(ctypes.byref(self._h), self.NC, self.NbC, self.NS,
+                                          self.NONZ, *[a.ctypes.data for a in ints],
+                                          *[a.ctypes.data for a in dbls], int(device))
+        if st != OK:
+            raise SolverError(st, last_error())
+
+    @classmethod
+    def from_faces(cls, msh, TypeBC, device=-1):
+        return cls(msh["NC"], msh["NbC"], msh["NS"], int(msh["Acol"][-1]), msh["SideC"],
+                   msh["SidAij"], msh["Adia"], TypeBC, msh, msh["volume"], device)
+
+    def calcps(self, fields, aval, b, abou, flux, Nmat=1, dt=1.0, errmax=True):
+        """Fill aval (NONZ), b (NC), abou (NbC, cells -NbC..-1) and flux (NS)
+        from the cell fields (CUDA float64 tensors over cells -NbC..NC,
+        keys FIELDS) on torch's current stream.  Returns {errmax, seconds}."""
+        for t in list(fields.values()) + [aval, b, abou, flux]:
+            if not (t.is_cuda and t.dtype.itemsize == 8 and t.is_contiguous()):
+                raise TypeError("fields and outputs must be contiguous CUDA float64 tensors")
+        F = _native.CalcpsFields(**{k: fields[k].data_ptr() for k in self.FIELDS})
+        em, sec = ctypes.c_double(), ctypes.c_double()
+        st = lib().tflows_calcps_assemble_device(self._h, int(Nmat), float(dt), ctypes.byref(F),
+                                                 _ptr(aval), _ptr(b), _ptr(abou), _ptr(flux),
+                                                 ctypes.byref(em) if errmax else None,
+                                                 _stream(), ctypes.byref(sec))
+        if st != OK:
+            raise SolverError(st, last_error())
+        return {"errmax": em.value if errmax else None, "seconds": sec.value}
+
+    def close(self):
+        if self._h:
+            lib().tflows_assembly_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,398 @@
+// Pressure-correction assembly on the GPU (Process/CalcPS.f90:49-202): the
+// face loop that fills Aval through SidAij and Adia, Abou and the face mass
+// fluxes, the right-hand side b, the density time-derivative source and the
+// removal of the volume-weighted mean of b.
+//
+// The reference runs one sequential loop over faces that scatters into the
+// diagonal and b of each face's two cells.  Here one thread per face computes
+// everything that depends on the face alone (A12, the flux, the off-diagonal
+// entries, Abou) and one thread per cell then adds its faces' contributions
+// in increasing face order (repeating the whole sequence Nmat times, as the
+// reference's `do m = 1, Nmat` does), from 0 as Aval(:) = 0 and b(:) = 0 do:
+// every cell sees the same operands in the same order, so Aval, Abou, the
+// fluxes and b before the mean removal are bit-identical to the sequential
+// loop (built with --fmad=false).  The mean sum_c b(c) volume(c) /
+// sum_c volume(c) is a deterministic tree reduction, not the reference's
+// left-to-right sum, so b differs from the reference by the rounding of that
+// one scalar.
+#include "internal.h"
+#include "tflows_krylov.h"
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+// Library/allp_mod.f90:16-24
+enum : int { kInflow = 1, kOutflow = 3, kConvect = 5, kBuffer = 11, kPressure = 12 };
+
+// What a face adds to its cells (set by the face pass, read by the cell pass).
+enum : unsigned char { kDiag1 = 1, kB1 = 2, kCell2 = 4 };
+
+constexpr int kAsmBlock = 256;
+
+struct FaceGeom {
+    const double* sx;
+    const double* sy;
+    const double* sz;
+    const double* dx;
+    const double* dy;
+    const double* dz;
+    const double* f;
+};
+
+struct CellFields {  // all over cells -NbC..NC, element c at [c + NbC]
+    const double* vol;
+    const double* asave;
+    const double* rho_n;
+    const double* rho_o;
+    const double* rho_oo;
+    const double* u;
+    const double* v;
+    const double* w;
+    const double* p;
+    const double* px;
+    const double* py;
+    const double* pz;
+    const int* type;
+};
+
+__device__ __forceinline__ double smdpn(const FaceGeom& g, int i) {
+    return (g.sx[i] * g.sx[i] + g.sy[i] * g.sy[i] + g.sz[i] * g.sz[i]) /
+           (g.sx[i] * g.dx[i] + g.sy[i] * g.dy[i] + g.sz[i] * g.dz[i]);
+}
+
+// One thread per face: CalcPS.f90:71-164 for face s = i + 1.
+__global__ void __launch_bounds__(kAsmBlock) face_kernel(int NS, int NbC, const int* __restrict__ c1s,
+                                                         const int* __restrict__ c2s,
+                                                         const int* __restrict__ sid1,
+                                                         const int* __restrict__ sid2, FaceGeom g,
+                                                         CellFields F, double* __restrict__ aval,
+                                                         double* __restrict__ abou,
+                                                         double* __restrict__ flux,
+                                                         double* __restrict__ a12s,
+                                                         unsigned char* __restrict__ kind) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NS; i += gridDim.x * blockDim.x) {
+        const int c1 = c1s[i] + NbC, c2 = c2s[i];
+        const int k2 = c2 + NbC;
+        const double f = g.f[i];
+        double A12 = 0.0, fl = 0.0;
+        unsigned char kd = 0;
+        const int t2 = c2 < 0 ? F.type[k2] : 0;
+        if (c2 > 0 || (c2 < 0 && t2 == kBuffer)) {
+            const double S = smdpn(g, i);
+            const double Urs = f * F.rho_n[c1] * F.u[c1] + (1.0 - f) * F.rho_n[k2] * F.u[k2];
+            const double Vrs = f * F.rho_n[c1] * F.v[c1] + (1.0 - f) * F.rho_n[k2] * F.v[k2];
+            const double Wrs = f * F.rho_n[c1] * F.w[c1] + (1.0 - f) * F.rho_n[k2] * F.w[k2];
+            A12 = 0.5 * S * (F.vol[c1] / F.asave[c1] + F.vol[k2] / F.asave[k2]);
+            if (c2 > 0) {
+                aval[sid1[i]] = -A12;
+                aval[sid2[i]] = -A12;
+                kd = kDiag1 | kB1 | kCell2;
+            } else {
+                abou[k2] = -A12;
+                kd = kDiag1 | kB1;
+            }
+            const double dPxi = .5 * (F.px[c1] + F.px[k2]) * g.dx[i];
+            const double dPyi = .5 * (F.py[c1] + F.py[k2]) * g.dy[i];
+            const double dPzi = .5 * (F.pz[c1] + F.pz[k2]) * g.dz[i];
+            fl = (Urs * g.sx[i] + Vrs * g.sy[i] + Wrs * g.sz[i]) + A12 * (F.p[c1] - F.p[k2]) +
+                 A12 * (dPxi + dPyi + dPzi);
+        } else if (t2 == kInflow || t2 == kOutflow || t2 == kConvect) {
+            const double Urs = f * F.rho_n[c1] * F.u[c1] + (1.0 - f) * F.rho_n[k2] * F.u[k2];
+            const double Vrs = f * F.rho_n[c1] * F.v[c1] + (1.0 - f) * F.rho_n[k2] * F.v[k2];
+            const double Wrs = f * F.rho_n[c1] * F.w[c1] + (1.0 - f) * F.rho_n[k2] * F.w[k2];
+            fl = (Urs * g.sx[i] + Vrs * g.sy[i] + Wrs * g.sz[i]);
+            kd = kB1;
+            if (t2 != kInflow) {  // OUTFLOW / CONVECT add A12 to the diagonal
+                A12 = smdpn(g, i) * F.vol[c1] / F.asave[c1];
+                kd |= kDiag1;
+            }
+        } else if (t2 == kPressure) {
+            const double Urs = F.rho_n[c1] * F.u[c1];
+            const double Vrs = F.rho_n[c1] * F.v[c1];
+            const double Wrs = F.rho_n[c1] * F.w[c1];
+            fl = (Urs * g.sx[i] + Vrs * g.sy[i] + Wrs * g.sz[i]);
+            A12 = smdpn(g, i) * F.vol[c1] / F.asave[c1];
+            kd = kB1 | kDiag1;
+        }  // every other type (walls, symmetry): Flux(s) = 0, nothing added
+        flux[i] = fl;
+        a12s[i] = A12;
+        kind[i] = kd;
+    }
+}
+
+// One thread per cell c = i + 1: its faces' contributions in face order,
+// Nmat times (CalcPS.f90:69-167), errmax (171-174), then the source
+// (186-193) and this cell's terms of the two sums of the mean.
+__global__ void __launch_bounds__(kAsmBlock) cell_kernel(
+    int NC, int NbC, int Nmat, double dt, const int* __restrict__ cf_ptr,
+    const int* __restrict__ cf, const int* __restrict__ adia, const double* __restrict__ a12s,
+    const double* __restrict__ flux, const unsigned char* __restrict__ kind, CellFields F,
+    double* __restrict__ aval, double* __restrict__ b, double* __restrict__ part_sum,
+    double* __restrict__ part_vol, unsigned long long* __restrict__ errmax_bits) {
+    __shared__ double s_sum[kAsmBlock / 32], s_vol[kAsmBlock / 32];
+    double my_sum = 0.0, my_vol = 0.0;
+    unsigned long long my_max = 0ull;
+    for (int base = blockIdx.x * blockDim.x; base < NC; base += gridDim.x * blockDim.x) {
+        const int i = base + threadIdx.x;
+        if (i < NC) {
+            const int e0 = cf_ptr[i], e1 = cf_ptr[i + 1];
+            double d = 0.0, bb = 0.0;
+            bool diag = false;
+            for (int m = 0; m < Nmat; ++m)
+                for (int e = e0; e < e1; ++e) {
+                    const int code = cf[e];
+                    const int s = code >> 1;
+                    const unsigned char kd = kind[s];
+                    if (code & 1) {  // this cell is the face's c2
+                        d = d + a12s[s];
+                        bb = bb + flux[s];
+                        diag = true;
+                    } else {
+                        if (kd & kDiag1) {
+                            d = d + a12s[s];
+                            diag = true;
+                        }
+                        if (kd & kB1) bb = bb - flux[s];
+                    }
+                }
+            if (diag) aval[adia[i]] = d;
+            my_max = max(my_max, (unsigned long long)__double_as_longlong(fabs(bb)));
+            const int c = i + 1 + NbC;
+            for (int m = 0; m < Nmat; ++m) {
+                bb = bb - F.vol[c] / dt * (1.5 * F.rho_n[c] - 2.0 * F.rho_o[c] + 0.5 * F.rho_oo[c]);
+                my_sum = my_sum + bb * F.vol[c];
+                my_vol = my_vol + F.vol[c];
+            }
+            b[i] = bb;
+        }
+    }
+    // block partial sums in a fixed order (deterministic)
+    for (int o = 16; o > 0; o >>= 1) {
+        my_sum += __shfl_down_sync(0xffffffffu, my_sum, o);
+        my_vol += __shfl_down_sync(0xffffffffu, my_vol, o);
+        my_max = max(my_max, __shfl_down_sync(0xffffffffu, my_max, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_sum[warp] = my_sum;
+        s_vol[warp] = my_vol;
+        atomicMax(errmax_bits, my_max);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            a += s_sum[w];
+            v += s_vol[w];
+        }
+        part_sum[blockIdx.x] = a;
+        part_vol[blockIdx.x] = v;
+    }
+}
+
+// b(c) = b(c) - bc_sum / vol (CalcPS.f90:199-202); every thread sums the
+// block partials in the same order.
+__global__ void __launch_bounds__(kAsmBlock) mean_kernel(int NC, int nparts,
+                                                         const double* __restrict__ part_sum,
+                                                         const double* __restrict__ part_vol,
+                                                         double* __restrict__ b,
+                                                         double* __restrict__ sums) {
+    __shared__ double s_shift;
+    if (threadIdx.x == 0) {
+        double a = 0.0, v = 0.0;
+        for (int k = 0; k < nparts; ++k) {
+            a += part_sum[k];
+            v += part_vol[k];
+        }
+        s_shift = a / v;
+        if (blockIdx.x == 0) {
+            sums[0] = a;
+            sums[1] = v;
+        }
+    }
+    __syncthreads();
+    const double shift = s_shift;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NC; i += gridDim.x * blockDim.x)
+        b[i] = b[i] - shift;
+}
+
+template <typename T>
+cudaError_t upload(T** dst, const T* src, size_t count) {
+    cudaError_t e = cudaMalloc((void**)dst, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess && count)
+        e = cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice);
+    return e;
+}
+
+int asm_fail(int status, const std::string& msg) { return tflows::report_status(status, msg); }
+
+}  // namespace
+
+struct tflows_assembly {
+    int device = 0;
+    int NC = 0, NbC = 0, NS = 0, NONZ = 0;
+    int nblocks = 0;
+    int *c1 = nullptr, *c2 = nullptr, *sid1 = nullptr, *sid2 = nullptr;
+    int *adia = nullptr, *type = nullptr, *cf_ptr = nullptr, *cf = nullptr;
+    double* geom = nullptr;  // Sx Sy Sz Dx Dy Dz f, NS each
+    double* vol = nullptr;   // -NbC..NC
+    double* a12 = nullptr;
+    unsigned char* kind = nullptr;
+    double* parts = nullptr;  // 2 * nblocks partial sums, then the two totals
+    unsigned long long* errmax = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+extern "C" {
+
+void tflows_assembly_destroy(tflows_assembly* a) {
+    if (!a) return;
+    cudaSetDevice(a->device);
+    for (void* p : {(void*)a->c1, (void*)a->c2, (void*)a->sid1, (void*)a->sid2, (void*)a->adia,
+                    (void*)a->type, (void*)a->cf_ptr, (void*)a->cf, (void*)a->geom, (void*)a->vol,
+                    (void*)a->a12, (void*)a->kind, (void*)a->parts, (void*)a->errmax})
+        if (p) cudaFree(p);
+    if (a->ev0) cudaEventDestroy(a->ev0);
+    if (a->ev1) cudaEventDestroy(a->ev1);
+    delete a;
+}
+
+int tflows_assembly_create(tflows_assembly** out, int NC, int NbC, int NS, int NONZ,
+                           const int* SideC, const int* SidAij, const int* Adia,
+                           const int* TypeBC, const double* Sx, const double* Sy,
+                           const double* Sz, const double* Dx, const double* Dy,
+                           const double* Dz, const double* f, const double* volume, int device) {
+    if (!out || NC <= 0 || NbC < 0 || NS < 0 || NONZ < 1 || !SideC || !SidAij || !Adia ||
+        !TypeBC || !Sx || !Sy || !Sz || !Dx || !Dy || !Dz || !f || !volume)
+        return asm_fail(TFLOWS_BAD_INPUT, "null argument or bad size");
+    // host-side checks: every index the kernels follow stays in range
+    std::vector<int> c1(NS), c2(NS), s1(NS), s2(NS);
+    std::vector<int> deg(NC + 1, 0);
+    for (int s = 0; s < NS; ++s) {
+        c1[s] = SideC[3 * s + 1];
+        c2[s] = SideC[3 * s + 2];
+        if (c1[s] < 1 || c1[s] > NC || c2[s] == 0 || c2[s] > NC || c2[s] < -NbC)
+            return asm_fail(TFLOWS_BAD_INPUT, "SideC out of range at face " + std::to_string(s + 1));
+        if (c2[s] > 0) {
+            s1[s] = SidAij[2 * s] - 1;
+            s2[s] = SidAij[2 * s + 1] - 1;
+            if (s1[s] < 0 || s1[s] >= NONZ || s2[s] < 0 || s2[s] >= NONZ)
+                return asm_fail(TFLOWS_BAD_INPUT, "SidAij out of range at face " + std::to_string(s + 1));
+            deg[c2[s]] += 1;
+        } else {
+            s1[s] = s2[s] = -1;
+        }
+        deg[c1[s]] += 1;
+    }
+    std::vector<int> adia(NC);
+    for (int c = 0; c < NC; ++c) {
+        adia[c] = Adia[c] - 1;
+        if (adia[c] < 0 || adia[c] >= NONZ) return asm_fail(TFLOWS_BAD_INPUT, "Adia out of range");
+    }
+    // cell -> faces in increasing face order; bit 0 = the cell is c2
+    std::vector<int> ptr(NC + 1, 0);
+    for (int c = 1; c <= NC; ++c) ptr[c] = ptr[c - 1] + deg[c];
+    std::vector<int> cf(std::max(ptr[NC], 1)), fill(ptr.begin(), ptr.end() - 1);
+    for (int s = 0; s < NS; ++s) {
+        cf[fill[c1[s] - 1]++] = 2 * s;
+        if (c2[s] > 0) cf[fill[c2[s] - 1]++] = 2 * s + 1;
+    }
+    if (device >= 0 && cudaSetDevice(device) != cudaSuccess)
+        return asm_fail(TFLOWS_NO_DEVICE, "cudaSetDevice failed");
+    auto* a = new tflows_assembly();
+    cudaGetDevice(&a->device);
+    a->NC = NC;
+    a->NbC = NbC;
+    a->NS = NS;
+    a->NONZ = NONZ;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, a->device);
+    a->nblocks = std::max(1, std::min((NC + kAsmBlock - 1) / kAsmBlock, 8 * std::max(sms, 1)));
+    std::vector<double> geom((size_t)7 * NS);
+    const double* src[7] = {Sx, Sy, Sz, Dx, Dy, Dz, f};
+    for (int k = 0; k < 7; ++k) std::memcpy(geom.data() + (size_t)k * NS, src[k], sizeof(double) * NS);
+    cudaError_t e = upload(&a->c1, c1.data(), NS);
+    if (e == cudaSuccess) e = upload(&a->c2, c2.data(), NS);
+    if (e == cudaSuccess) e = upload(&a->sid1, s1.data(), NS);
+    if (e == cudaSuccess) e = upload(&a->sid2, s2.data(), NS);
+    if (e == cudaSuccess) e = upload(&a->adia, adia.data(), NC);
+    if (e == cudaSuccess) e = upload(&a->type, TypeBC, (size_t)NbC + NC + 1);
+    if (e == cudaSuccess) e = upload(&a->cf_ptr, ptr.data(), ptr.size());
+    if (e == cudaSuccess) e = upload(&a->cf, cf.data(), cf.size());
+    if (e == cudaSuccess) e = upload(&a->geom, geom.data(), geom.size());
+    if (e == cudaSuccess) e = upload(&a->vol, volume, (size_t)NbC + NC + 1);
+    if (e == cudaSuccess) e = cudaMalloc(&a->a12, sizeof(double) * std::max(NS, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&a->kind, std::max(NS, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&a->parts, sizeof(double) * (2 * a->nblocks + 2));
+    if (e == cudaSuccess) e = cudaMalloc(&a->errmax, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaEventCreate(&a->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&a->ev1);
+    if (e != cudaSuccess) {
+        tflows_assembly_destroy(a);
+        return asm_fail(TFLOWS_CUDA_ERROR, std::string("assembly set-up: ") + cudaGetErrorString(e));
+    }
+    *out = a;
+    return asm_fail(TFLOWS_OK, "");
+}
+
+int tflows_calcps_assemble_device(tflows_assembly* a, int Nmat, double dt,
+                                  const tflows_calcps_fields* in, double* aval, double* b,
+                                  double* abou, double* flux, double* errmax, void* stream,
+                                  double* seconds) {
+    if (!a || !in || !aval || !b || !flux || (a->NbC > 0 && !abou))
+        return asm_fail(TFLOWS_BAD_INPUT, "null argument");
+    if (Nmat < 1) return asm_fail(TFLOWS_BAD_INPUT, "Nmat must be >= 1");
+    const double* fl[11] = {in->rho_n, in->rho_o, in->rho_oo, in->u, in->v, in->w,
+                            in->p, in->px, in->py, in->pz, in->asave};
+    for (const double* p : fl)
+        if (!p) return asm_fail(TFLOWS_BAD_INPUT, "null field");
+    cudaSetDevice(a->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    FaceGeom g{a->geom, a->geom + a->NS, a->geom + 2 * (size_t)a->NS, a->geom + 3 * (size_t)a->NS,
+               a->geom + 4 * (size_t)a->NS, a->geom + 5 * (size_t)a->NS,
+               a->geom + 6 * (size_t)a->NS};
+    CellFields F{a->vol, in->asave, in->rho_n, in->rho_o, in->rho_oo, in->u, in->v,
+                 in->w, in->p, in->px, in->py, in->pz, a->type};
+    cudaEventRecord(a->ev0, s);
+    cudaError_t e = cudaMemsetAsync(aval, 0, sizeof(double) * a->NONZ, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a->errmax, 0, sizeof(unsigned long long), s);
+    const int fb = std::max(1, std::min((a->NS + kAsmBlock - 1) / kAsmBlock, 65535));
+    if (e == cudaSuccess && a->NS > 0) {
+        face_kernel<<<fb, kAsmBlock, 0, s>>>(a->NS, a->NbC, a->c1, a->c2, a->sid1, a->sid2, g, F,
+                                             aval, abou, flux, a->a12, a->kind);
+        e = cudaGetLastError();
+    }
+    double* ps = a->parts;
+    double* pv = a->parts + a->nblocks;
+    double* tot = a->parts + 2 * a->nblocks;
+    if (e == cudaSuccess) {
+        cell_kernel<<<a->nblocks, kAsmBlock, 0, s>>>(a->NC, a->NbC, Nmat, dt, a->cf_ptr, a->cf,
+                                                     a->adia, a->a12, flux, a->kind, F, aval, b,
+                                                     ps, pv, a->errmax);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        mean_kernel<<<a->nblocks, kAsmBlock, 0, s>>>(a->NC, a->nblocks, ps, pv, b, tot);
+        e = cudaGetLastError();
+    }
+    cudaEventRecord(a->ev1, s);
+    unsigned long long bits = 0;
+    if (e == cudaSuccess && errmax)
+        e = cudaMemcpyAsync(&bits, a->errmax, sizeof(bits), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && (errmax || seconds)) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return asm_fail(TFLOWS_CUDA_ERROR, std::string("assembly: ") + cudaGetErrorString(e));
+    if (errmax) std::memcpy(errmax, &bits, sizeof(double));
+    if (seconds) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a->ev0, a->ev1);
+        *seconds = ms * 1e-3;
+    }
+    return asm_fail(TFLOWS_OK, "");
+}
+
+}  // extern "C"

@@ -147,6 +147,9 @@ cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, do
 cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, const double* x,
                               double* g, cudaStream_t s);
 
+// Records the status and message tflows_last_status / tflows_last_error report.
+int report_status(int status, const std::string& msg);
+
 // The persistent kernels, built twice: krylov.cu with the reference's
 // arithmetic (separate rounded products and sums, dividing diagonal) and
 // krylov_fma.cu with fused multiply-adds (TFLOWS_FP64_FMA and mixed solves).

@@ -506,6 +506,13 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
 
 }  // namespace
 
+// Status and message of the last call on this thread, for the other units.
+int tflows::report_status(int status, const std::string& msg) {
+    t_status = status;
+    t_error = msg;
+    return status;
+}
+
 extern "C" {
 
 void tflows_default_options(tflows_options* opt) {
