@@ -457,6 +457,72 @@ def simple_step(pkg, dev, n=128, reps=3, autotune=True):
             "group_blocks": [r["grid_blocks"] for r in res], "tuning": tuning}
 
 
+def assembly_block(pkg, dev, n=128, reps=5):
+    """The pressure-correction assembly (Process/CalcPS.f90:49-202) of an
+    n^3 perturbed box on the GPU: inflow on x-min, outflow on x-max, walls
+    elsewhere, seeded fields.  Reports the device time, the algorithmic bytes
+    (every input read once, every output written once) against the HBM peak,
+    and the host->device copy of Aval and b it makes unnecessary when the
+    fields live on the GPU; the CPU restatement (one core) beside it."""
+    import numpy as np
+    import torch
+    import oracle
+    msh = pkg.mesh.box_faces(n, n, n, perturb=0.2, seed=7)
+    NC, NbC, NS = msh["NC"], msh["NbC"], msh["NS"]
+    NONZ = int(msh["Acol"][-1])
+    rng = np.random.default_rng(8)
+    m = NbC + NC + 1
+    tb = np.full(m, 2, np.int32)
+    tb[NbC:] = 0
+    ny = nz = n
+    tb[NbC - np.arange(1, ny * nz + 1)] = 1           # x-min walls: inflow (cells -1..)
+    tb[NbC - np.arange(ny * nz + 1, 2 * ny * nz + 1)] = 3  # x-max: outflow
+    cpu = {"volume": msh["volume"], "Asave": rng.uniform(1.0, 2.0, m)}
+    for k in ("rho_n", "rho_o", "rho_oo"):
+        cpu[k] = rng.uniform(0.5, 1.5, m)
+    for k in ("U", "V", "W", "P", "Px", "Py", "Pz"):
+        cpu[k] = rng.uniform(-1.0, 1.0, m)
+    asm = pkg.Assembly.from_faces(msh, tb)
+    key = {"rho_n": "rho_n", "rho_o": "rho_o", "rho_oo": "rho_oo", "u": "U", "v": "V", "w": "W",
+           "p": "P", "px": "Px", "py": "Py", "pz": "Pz", "asave": "Asave"}
+    fields = {k: torch.from_numpy(cpu[v]).to(dev) for k, v in key.items()}
+    aval = torch.empty(NONZ, dtype=torch.float64, device=dev)
+    b = torch.empty(NC, dtype=torch.float64, device=dev)
+    abou = torch.zeros(NbC, dtype=torch.float64, device=dev)
+    flux = torch.empty(NS, dtype=torch.float64, device=dev)
+    secs = []
+    for _ in range(reps + 2):
+        secs.append(asm.calcps(fields, aval, b, abou, flux, Nmat=1, dt=0.01)["seconds"])
+    sec = min(secs[2:])
+    # what the assembly reads and writes once: geometry 7 doubles + 4 ints per
+    # face, 12 cell arrays + TypeBC + Adia, outputs Aval, b, Flux
+    byts = NS * (7 * 8 + 4 * 4) + m * (12 * 8 + 4) + NC * 4 + 8 * (NONZ + NC + NS)
+    # the copy it replaces: Aval and b from pinned host memory
+    h = torch.empty(NONZ + NC, dtype=torch.float64).pin_memory()
+    dd = torch.empty_like(h, device=dev)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    dd.copy_(h, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    h2d = e0.elapsed_time(e1) * 1e-3
+    gpu_aval = aval.cpu().numpy()
+    t0 = time.perf_counter()
+    ref = oracle.calcps_assembly(NC, NbC, NS, NONZ, 1, 0.01, msh["SideC"], msh["SidAij"],
+                                 msh["Adia"], tb, {k: msh[k] for k in oracle.FACE_GEOM},
+                                 {k: cpu[k] for k in oracle.CELL_FIELDS})
+    cpu_s = time.perf_counter() - t0
+    same = bool(np.array_equal(gpu_aval.view(np.uint64), ref[0].view(np.uint64)))
+    asm.close()
+    peak, _ = load_peaks()
+    return {"workload": f"CalcPS assembly, {n}^3 perturbed box ({NC} cells, {NS} faces), "
+                        "inflow/outflow/walls, Nmat 1",
+            "ms": sec * 1e3, "gbs": byts / sec / 1e9, "frac": byts / sec / 1e9 / peak,
+            "algorithmic_bytes": byts, "h2d_aval_b_ms": h2d * 1e3,
+            "cpu_oracle_ms": cpu_s * 1e3, "cpu_cores": 1, "aval_bitwise_vs_oracle": same}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -608,6 +674,8 @@ def main():
         line["adjoint_cfg5"] = adjoint_cfg5(pkg, dev)
         torch.cuda.empty_cache()
         line["simple_step"] = simple_step(pkg, dev, autotune=not args.no_autotune)
+        torch.cuda.empty_cache()
+        line["assembly_calcps"] = assembly_block(pkg, dev)
         torch.cuda.empty_cache()
 
     if rank == 0 and (args.compare_scale or args.ic_compare_scale):
