@@ -41,10 +41,13 @@ struct FaceGeom {
     const double* dy;
     const double* dz;
     const double* f;
+    const double* smdpn;  // |S|^2 / (S.d), fixed with the mesh
+    const double* omf;    // 1.0 - f
 };
 
 struct CellFields {  // all over cells -NbC..NC, element c at [c + NbC]
     const double* vol;
+    const double* vdiva;  // volume / Asave of this call
     const double* asave;
     const double* rho_n;
     const double* rho_o;
@@ -59,34 +62,59 @@ struct CellFields {  // all over cells -NbC..NC, element c at [c + NbC]
     const int* type;
 };
 
-__device__ __forceinline__ double smdpn(const FaceGeom& g, int i) {
-    return (g.sx[i] * g.sx[i] + g.sy[i] * g.sy[i] + g.sz[i] * g.sz[i]) /
-           (g.sx[i] * g.dx[i] + g.sy[i] * g.dy[i] + g.sz[i] * g.dz[i]);
+// Quantities the face loop recomputes per face although they depend on the
+// mesh only (SMDPN, 1 - f) or on one cell only (volume / Asave) are formed
+// once, with the same operations, so the face pass is bit-identical to the
+// reference's and does a third of its FP64 work (the divides dominate).
+__global__ void __launch_bounds__(kAsmBlock) geom_kernel(int NS, const double* __restrict__ sx,
+                                                         const double* __restrict__ sy,
+                                                         const double* __restrict__ sz,
+                                                         const double* __restrict__ dx,
+                                                         const double* __restrict__ dy,
+                                                         const double* __restrict__ dz,
+                                                         const double* __restrict__ f,
+                                                         double* __restrict__ smdpn,
+                                                         double* __restrict__ omf) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NS; i += gridDim.x * blockDim.x) {
+        smdpn[i] = (sx[i] * sx[i] + sy[i] * sy[i] + sz[i] * sz[i]) /
+                   (sx[i] * dx[i] + sy[i] * dy[i] + sz[i] * dz[i]);
+        omf[i] = 1.0 - f[i];
+    }
+}
+
+__global__ void __launch_bounds__(kAsmBlock) vdiva_kernel(int n, const double* __restrict__ vol,
+                                                          const double* __restrict__ asave,
+                                                          double* __restrict__ q) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        q[i] = vol[i] / asave[i];
 }
 
 // One thread per face: CalcPS.f90:71-164 for face s = i + 1.
 __global__ void __launch_bounds__(kAsmBlock) face_kernel(int NS, int NbC, const int* __restrict__ c1s,
                                                          const int* __restrict__ c2s,
                                                          const int* __restrict__ sid1,
-                                                         const int* __restrict__ sid2, FaceGeom g,
+                                                         const int* __restrict__ sid2,
+                                                         const int* __restrict__ pos1,
+                                                         const int* __restrict__ pos2, FaceGeom g,
                                                          CellFields F, double* __restrict__ aval,
                                                          double* __restrict__ abou,
                                                          double* __restrict__ flux,
-                                                         double* __restrict__ a12s,
-                                                         unsigned char* __restrict__ kind) {
+                                                         double* __restrict__ slot_a,
+                                                         double* __restrict__ slot_f,
+                                                         unsigned char* __restrict__ slot_k) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NS; i += gridDim.x * blockDim.x) {
         const int c1 = c1s[i] + NbC, c2 = c2s[i];
         const int k2 = c2 + NbC;
-        const double f = g.f[i];
+        const double f = g.f[i], omf = g.omf[i];
         double A12 = 0.0, fl = 0.0;
         unsigned char kd = 0;
         const int t2 = c2 < 0 ? F.type[k2] : 0;
         if (c2 > 0 || (c2 < 0 && t2 == kBuffer)) {
-            const double S = smdpn(g, i);
-            const double Urs = f * F.rho_n[c1] * F.u[c1] + (1.0 - f) * F.rho_n[k2] * F.u[k2];
-            const double Vrs = f * F.rho_n[c1] * F.v[c1] + (1.0 - f) * F.rho_n[k2] * F.v[k2];
-            const double Wrs = f * F.rho_n[c1] * F.w[c1] + (1.0 - f) * F.rho_n[k2] * F.w[k2];
-            A12 = 0.5 * S * (F.vol[c1] / F.asave[c1] + F.vol[k2] / F.asave[k2]);
+            const double S = g.smdpn[i];
+            const double Urs = f * F.rho_n[c1] * F.u[c1] + omf * F.rho_n[k2] * F.u[k2];
+            const double Vrs = f * F.rho_n[c1] * F.v[c1] + omf * F.rho_n[k2] * F.v[k2];
+            const double Wrs = f * F.rho_n[c1] * F.w[c1] + omf * F.rho_n[k2] * F.w[k2];
+            A12 = 0.5 * S * (F.vdiva[c1] + F.vdiva[k2]);
             if (c2 > 0) {
                 aval[sid1[i]] = -A12;
                 aval[sid2[i]] = -A12;
@@ -101,13 +129,14 @@ __global__ void __launch_bounds__(kAsmBlock) face_kernel(int NS, int NbC, const 
             fl = (Urs * g.sx[i] + Vrs * g.sy[i] + Wrs * g.sz[i]) + A12 * (F.p[c1] - F.p[k2]) +
                  A12 * (dPxi + dPyi + dPzi);
         } else if (t2 == kInflow || t2 == kOutflow || t2 == kConvect) {
-            const double Urs = f * F.rho_n[c1] * F.u[c1] + (1.0 - f) * F.rho_n[k2] * F.u[k2];
-            const double Vrs = f * F.rho_n[c1] * F.v[c1] + (1.0 - f) * F.rho_n[k2] * F.v[k2];
-            const double Wrs = f * F.rho_n[c1] * F.w[c1] + (1.0 - f) * F.rho_n[k2] * F.w[k2];
+            const double Urs = f * F.rho_n[c1] * F.u[c1] + omf * F.rho_n[k2] * F.u[k2];
+            const double Vrs = f * F.rho_n[c1] * F.v[c1] + omf * F.rho_n[k2] * F.v[k2];
+            const double Wrs = f * F.rho_n[c1] * F.w[c1] + omf * F.rho_n[k2] * F.w[k2];
             fl = (Urs * g.sx[i] + Vrs * g.sy[i] + Wrs * g.sz[i]);
             kd = kB1;
             if (t2 != kInflow) {  // OUTFLOW / CONVECT add A12 to the diagonal
-                A12 = smdpn(g, i) * F.vol[c1] / F.asave[c1];
+                // SMDPN * volume(c1) / Asave(c1): a product then a divide
+                A12 = g.smdpn[i] * F.vol[c1] / F.asave[c1];
                 kd |= kDiag1;
             }
         } else if (t2 == kPressure) {
@@ -115,22 +144,33 @@ __global__ void __launch_bounds__(kAsmBlock) face_kernel(int NS, int NbC, const 
             const double Vrs = F.rho_n[c1] * F.v[c1];
             const double Wrs = F.rho_n[c1] * F.w[c1];
             fl = (Urs * g.sx[i] + Vrs * g.sy[i] + Wrs * g.sz[i]);
-            A12 = smdpn(g, i) * F.vol[c1] / F.asave[c1];
+            A12 = g.smdpn[i] * F.vol[c1] / F.asave[c1];
             kd = kB1 | kDiag1;
         }  // every other type (walls, symmetry): Flux(s) = 0, nothing added
         flux[i] = fl;
-        a12s[i] = A12;
-        kind[i] = kd;
+        // the face's entries in its cells' contribution lists
+        const int p1 = pos1[i];
+        slot_a[p1] = A12;
+        slot_f[p1] = fl;
+        slot_k[p1] = kd & (kDiag1 | kB1);
+        if (c2 > 0) {
+            const int p2 = pos2[i];
+            slot_a[p2] = A12;
+            slot_f[p2] = fl;
+            slot_k[p2] = kCell2;
+        }
     }
 }
 
 // One thread per cell c = i + 1: its faces' contributions in face order,
 // Nmat times (CalcPS.f90:69-167), errmax (171-174), then the source
-// (186-193) and this cell's terms of the two sums of the mean.
+// (186-193) and this cell's terms of the two sums of the mean.  The face
+// pass left each contribution in the cell's own list (entries cf_ptr[i] ..
+// cf_ptr[i+1]-1, faces in increasing order), so the reads are contiguous.
 __global__ void __launch_bounds__(kAsmBlock) cell_kernel(
     int NC, int NbC, int Nmat, double dt, const int* __restrict__ cf_ptr,
-    const int* __restrict__ cf, const int* __restrict__ adia, const double* __restrict__ a12s,
-    const double* __restrict__ flux, const unsigned char* __restrict__ kind, CellFields F,
+    const int* __restrict__ adia, const double* __restrict__ slot_a,
+    const double* __restrict__ slot_f, const unsigned char* __restrict__ slot_k, CellFields F,
     double* __restrict__ aval, double* __restrict__ b, double* __restrict__ part_sum,
     double* __restrict__ part_vol, unsigned long long* __restrict__ errmax_bits) {
     __shared__ double s_sum[kAsmBlock / 32], s_vol[kAsmBlock / 32];
@@ -144,19 +184,17 @@ __global__ void __launch_bounds__(kAsmBlock) cell_kernel(
             bool diag = false;
             for (int m = 0; m < Nmat; ++m)
                 for (int e = e0; e < e1; ++e) {
-                    const int code = cf[e];
-                    const int s = code >> 1;
-                    const unsigned char kd = kind[s];
-                    if (code & 1) {  // this cell is the face's c2
-                        d = d + a12s[s];
-                        bb = bb + flux[s];
+                    const unsigned char kd = slot_k[e];
+                    if (kd & kCell2) {  // this cell is the face's c2
+                        d = d + slot_a[e];
+                        bb = bb + slot_f[e];
                         diag = true;
                     } else {
                         if (kd & kDiag1) {
-                            d = d + a12s[s];
+                            d = d + slot_a[e];
                             diag = true;
                         }
-                        if (kd & kB1) bb = bb - flux[s];
+                        if (kd & kB1) bb = bb - slot_f[e];
                     }
                 }
             if (diag) aval[adia[i]] = d;
@@ -237,11 +275,13 @@ struct tflows_assembly {
     int NC = 0, NbC = 0, NS = 0, NONZ = 0;
     int nblocks = 0;
     int *c1 = nullptr, *c2 = nullptr, *sid1 = nullptr, *sid2 = nullptr;
-    int *adia = nullptr, *type = nullptr, *cf_ptr = nullptr, *cf = nullptr;
-    double* geom = nullptr;  // Sx Sy Sz Dx Dy Dz f, NS each
+    int *adia = nullptr, *type = nullptr, *cf_ptr = nullptr, *pos1 = nullptr, *pos2 = nullptr;
+    double* geom = nullptr;  // Sx Sy Sz Dx Dy Dz f SMDPN (1-f), NS each
     double* vol = nullptr;   // -NbC..NC
-    double* a12 = nullptr;
-    unsigned char* kind = nullptr;
+    double* vdiva = nullptr; // volume / Asave of the current call, -NbC..NC
+    double* slot_a = nullptr;  // per (cell, face): A12 and the flux the face adds
+    double* slot_f = nullptr;
+    unsigned char* slot_k = nullptr;
     double* parts = nullptr;  // 2 * nblocks partial sums, then the two totals
     unsigned long long* errmax = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -253,8 +293,9 @@ void tflows_assembly_destroy(tflows_assembly* a) {
     if (!a) return;
     cudaSetDevice(a->device);
     for (void* p : {(void*)a->c1, (void*)a->c2, (void*)a->sid1, (void*)a->sid2, (void*)a->adia,
-                    (void*)a->type, (void*)a->cf_ptr, (void*)a->cf, (void*)a->geom, (void*)a->vol,
-                    (void*)a->a12, (void*)a->kind, (void*)a->parts, (void*)a->errmax})
+                    (void*)a->type, (void*)a->cf_ptr, (void*)a->pos1, (void*)a->pos2,
+                    (void*)a->geom, (void*)a->vol, (void*)a->slot_a, (void*)a->slot_f,
+                    (void*)a->slot_k, (void*)a->parts, (void*)a->errmax, (void*)a->vdiva})
         if (p) cudaFree(p);
     if (a->ev0) cudaEventDestroy(a->ev0);
     if (a->ev1) cudaEventDestroy(a->ev1);
@@ -293,14 +334,17 @@ int tflows_assembly_create(tflows_assembly** out, int NC, int NbC, int NS, int N
         adia[c] = Adia[c] - 1;
         if (adia[c] < 0 || adia[c] >= NONZ) return asm_fail(TFLOWS_BAD_INPUT, "Adia out of range");
     }
-    // cell -> faces in increasing face order; bit 0 = the cell is c2
+    // each cell's faces in increasing face order: the entry of face s in the
+    // list of its c1 (pos1) and of its c2 (pos2, interior faces)
     std::vector<int> ptr(NC + 1, 0);
     for (int c = 1; c <= NC; ++c) ptr[c] = ptr[c - 1] + deg[c];
-    std::vector<int> cf(std::max(ptr[NC], 1)), fill(ptr.begin(), ptr.end() - 1);
+    std::vector<int> pos1(std::max(NS, 1)), pos2(std::max(NS, 1), -1);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
     for (int s = 0; s < NS; ++s) {
-        cf[fill[c1[s] - 1]++] = 2 * s;
-        if (c2[s] > 0) cf[fill[c2[s] - 1]++] = 2 * s + 1;
+        pos1[s] = fill[c1[s] - 1]++;
+        if (c2[s] > 0) pos2[s] = fill[c2[s] - 1]++;
     }
+    const size_t nslot = std::max(ptr[NC], 1);
     if (device >= 0 && cudaSetDevice(device) != cudaSuccess)
         return asm_fail(TFLOWS_NO_DEVICE, "cudaSetDevice failed");
     auto* a = new tflows_assembly();
@@ -312,7 +356,7 @@ int tflows_assembly_create(tflows_assembly** out, int NC, int NbC, int NS, int N
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, a->device);
     a->nblocks = std::max(1, std::min((NC + kAsmBlock - 1) / kAsmBlock, 8 * std::max(sms, 1)));
-    std::vector<double> geom((size_t)7 * NS);
+    std::vector<double> geom((size_t)9 * NS);
     const double* src[7] = {Sx, Sy, Sz, Dx, Dy, Dz, f};
     for (int k = 0; k < 7; ++k) std::memcpy(geom.data() + (size_t)k * NS, src[k], sizeof(double) * NS);
     cudaError_t e = upload(&a->c1, c1.data(), NS);
@@ -322,11 +366,23 @@ int tflows_assembly_create(tflows_assembly** out, int NC, int NbC, int NS, int N
     if (e == cudaSuccess) e = upload(&a->adia, adia.data(), NC);
     if (e == cudaSuccess) e = upload(&a->type, TypeBC, (size_t)NbC + NC + 1);
     if (e == cudaSuccess) e = upload(&a->cf_ptr, ptr.data(), ptr.size());
-    if (e == cudaSuccess) e = upload(&a->cf, cf.data(), cf.size());
+    if (e == cudaSuccess) e = upload(&a->pos1, pos1.data(), pos1.size());
+    if (e == cudaSuccess) e = upload(&a->pos2, pos2.data(), pos2.size());
     if (e == cudaSuccess) e = upload(&a->geom, geom.data(), geom.size());
     if (e == cudaSuccess) e = upload(&a->vol, volume, (size_t)NbC + NC + 1);
-    if (e == cudaSuccess) e = cudaMalloc(&a->a12, sizeof(double) * std::max(NS, 1));
-    if (e == cudaSuccess) e = cudaMalloc(&a->kind, std::max(NS, 1));
+    if (e == cudaSuccess && NS > 0) {
+        double* G = a->geom;
+        const size_t ns = NS;
+        geom_kernel<<<std::max(1, std::min((NS + kAsmBlock - 1) / kAsmBlock, 65535)), kAsmBlock>>>(
+            NS, G, G + ns, G + 2 * ns, G + 3 * ns, G + 4 * ns, G + 5 * ns, G + 6 * ns, G + 7 * ns,
+            G + 8 * ns);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&a->vdiva, sizeof(double) * ((size_t)NbC + NC + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&a->slot_a, sizeof(double) * nslot);
+    if (e == cudaSuccess) e = cudaMalloc(&a->slot_f, sizeof(double) * nslot);
+    if (e == cudaSuccess) e = cudaMalloc(&a->slot_k, nslot);
     if (e == cudaSuccess) e = cudaMalloc(&a->parts, sizeof(double) * (2 * a->nblocks + 2));
     if (e == cudaSuccess) e = cudaMalloc(&a->errmax, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaEventCreate(&a->ev0);
@@ -352,26 +408,34 @@ int tflows_calcps_assemble_device(tflows_assembly* a, int Nmat, double dt,
         if (!p) return asm_fail(TFLOWS_BAD_INPUT, "null field");
     cudaSetDevice(a->device);
     cudaStream_t s = (cudaStream_t)stream;
-    FaceGeom g{a->geom, a->geom + a->NS, a->geom + 2 * (size_t)a->NS, a->geom + 3 * (size_t)a->NS,
-               a->geom + 4 * (size_t)a->NS, a->geom + 5 * (size_t)a->NS,
-               a->geom + 6 * (size_t)a->NS};
-    CellFields F{a->vol, in->asave, in->rho_n, in->rho_o, in->rho_oo, in->u, in->v,
+    const size_t ns = a->NS;
+    FaceGeom g{a->geom,          a->geom + ns,     a->geom + 2 * ns,
+               a->geom + 3 * ns, a->geom + 4 * ns, a->geom + 5 * ns,
+               a->geom + 6 * ns, a->geom + 7 * ns, a->geom + 8 * ns};
+    CellFields F{a->vol, a->vdiva, in->asave, in->rho_n, in->rho_o, in->rho_oo, in->u, in->v,
                  in->w, in->p, in->px, in->py, in->pz, a->type};
     cudaEventRecord(a->ev0, s);
     cudaError_t e = cudaMemsetAsync(aval, 0, sizeof(double) * a->NONZ, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(a->errmax, 0, sizeof(unsigned long long), s);
+    const int ncell = a->NbC + a->NC + 1;
+    if (e == cudaSuccess) {
+        vdiva_kernel<<<std::max(1, std::min((ncell + kAsmBlock - 1) / kAsmBlock, 65535)), kAsmBlock,
+                       0, s>>>(ncell, a->vol, in->asave, a->vdiva);
+        e = cudaGetLastError();
+    }
     const int fb = std::max(1, std::min((a->NS + kAsmBlock - 1) / kAsmBlock, 65535));
     if (e == cudaSuccess && a->NS > 0) {
-        face_kernel<<<fb, kAsmBlock, 0, s>>>(a->NS, a->NbC, a->c1, a->c2, a->sid1, a->sid2, g, F,
-                                             aval, abou, flux, a->a12, a->kind);
+        face_kernel<<<fb, kAsmBlock, 0, s>>>(a->NS, a->NbC, a->c1, a->c2, a->sid1, a->sid2,
+                                             a->pos1, a->pos2, g, F, aval, abou, flux,
+                                             a->slot_a, a->slot_f, a->slot_k);
         e = cudaGetLastError();
     }
     double* ps = a->parts;
     double* pv = a->parts + a->nblocks;
     double* tot = a->parts + 2 * a->nblocks;
     if (e == cudaSuccess) {
-        cell_kernel<<<a->nblocks, kAsmBlock, 0, s>>>(a->NC, a->NbC, Nmat, dt, a->cf_ptr, a->cf,
-                                                     a->adia, a->a12, flux, a->kind, F, aval, b,
+        cell_kernel<<<a->nblocks, kAsmBlock, 0, s>>>(a->NC, a->NbC, Nmat, dt, a->cf_ptr, a->adia,
+                                                     a->slot_a, a->slot_f, a->slot_k, F, aval, b,
                                                      ps, pv, a->errmax);
         e = cudaGetLastError();
     }
