@@ -260,6 +260,35 @@ int tflows_spmv_device(tflows_topology *topo, const double *val,
                        const double *x, double *y, int repeat, int fp32,
                        void *stream, double *sec);
 
+/* ---- T-FlowS mesh files ---------------------------------------------------- */
+/* A mesh as the solver loads it: NAME.cns (Process/CnsLoa.f90) and NAME.geo
+ * (Library/GeoLoa.f90), gfortran sequential unformatted files (4-byte record
+ * markers, 4-byte INTEGER, 8-byte REAL, native byte order).  Arrays the
+ * reference declares over (-NbC:NC) point at element -NbC; bcmark and CopyC
+ * (-NbC:-1) at -NbC; SideC is SideC(0:2,NS) column-major; volume, delta,
+ * WallDs (1:NC); face arrays (1:NS).  Geometry pointers are NULL when no
+ * .geo file was given. */
+typedef struct tflows_mesh {
+    int NC, NbC, NS, NSsh, Nmat;
+    int *material, *SideC, *bcmark, *CopyC;
+    double *xc, *yc, *zc;
+    double *volume, *delta, *WallDs;
+    double *Sx, *Sy, *Sz, *Dx, *Dy, *Dz, *f, *xsp, *ysp, *zsp;
+} tflows_mesh;
+/* Reads the files (geo_path may be NULL); TFLOWS_BAD_INPUT with a message
+ * naming the record on a short, truncated or inconsistent file. */
+int tflows_mesh_read(const char *cns_path, const char *geo_path,
+                     tflows_mesh **out);
+void tflows_mesh_free(tflows_mesh *m);
+/* Process/TopolM.f90:24-98: the compressed-row layout of the face list
+ * SideC(0:2,NS): *NONZ <- stored entries + 1; with Acol (NC+1), Arow
+ * (NONZ), Adia (NC) given (else a size query) the 1-based row pointers,
+ * ascending column indices and diagonal positions; with SidAij (2*NS) given
+ * the positions of each interior face's (c1,c2) and (c2,c1) entries (0 on
+ * boundary faces). */
+int tflows_topolm(int NC, int NS, const int *SideC, int *Acol, int *Arow,
+                  int *Adia, int *SidAij, int *NONZ);
+
 /* ---- pressure-correction assembly on the GPU ------------------------------ */
 /* Mesh data of the assembly, resident on the device (host arrays in, copied):
  * SideC(0:2,NS) and SidAij(2,NS) as the reference holds them (column-major),

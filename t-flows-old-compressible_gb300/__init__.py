@@ -13,5 +13,5 @@ from .api import (  # noqa: F401
     BAD_INPUT, BICG, BICG_TRUE, BREAKDOWN, CG, CGS, CUDA_ERROR, FP64, FP64_FMA, MIXED, NO_DEVICE, NONFINITE,
     NOT_CONVERGED, OK, TIMEOUT, TOL_ABSOLUTE, TOL_RELATIVE, UNSUPPORTED, SolveOutput, SolverError,
     Assembly, Plan, Topology, autotune_clear, bicg, cg, cgs, finalize, last_error, last_result, last_status, options, prec1, resid,
-    set_options, solve_batched, solve_ex, solve_system, status_string,
+    read_mesh, set_options, solve_batched, solve_ex, solve_system, status_string, topolm,
 )

@@ -18,7 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libtflows_krylov.so")
-SOURCES = ("krylov.cu", "krylov_fma.cu", "shim.cu", "noalloc.cu", "tune.cu", "assembly.cu")
+SOURCES = ("krylov.cu", "krylov_fma.cu", "shim.cu", "noalloc.cu", "tune.cu", "assembly.cu",
+           "meshio.cpp")
 HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "solver_entry.cuh", "internal.h")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -59,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cc = nvcc()
 
         def compile_one(src):
-            obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+            obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
             extra = os.environ.get("TFLOWS_NVCC_EXTRA", "").split()
             # the contracted build fuses multiply-adds; everything else keeps
             # the reference's separately rounded products and sums
@@ -132,6 +133,15 @@ class BatchTuning(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Mesh(ctypes.Structure):
+    _fields_ = ([(n, ctypes.c_int) for n in ("NC", "NbC", "NS", "NSsh", "Nmat")]
+                + [(n, ctypes.POINTER(ctypes.c_int)) for n in ("material", "SideC", "bcmark",
+                                                              "CopyC")]
+                + [(n, ctypes.POINTER(ctypes.c_double))
+                   for n in ("xc", "yc", "zc", "volume", "delta", "WallDs", "Sx", "Sy", "Sz",
+                             "Dx", "Dy", "Dz", "f", "xsp", "ysp", "zsp")])
+
+
 class CalcpsFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("rho_n", "rho_o", "rho_oo", "u", "v", "w", "p",
                                                  "px", "py", "pz", "asave")]
@@ -182,6 +192,10 @@ SIGNATURES = {
                                        ctypes.POINTER(CalcpsFields), _VP, _VP, _VP, _VP,
                                        ctypes.POINTER(ctypes.c_double), _VP,
                                        ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "tflows_mesh_read": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(Mesh))],
+                         ctypes.c_int),
+    "tflows_mesh_free": ([ctypes.POINTER(Mesh)], None),
+    "tflows_topolm": ([ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _I], ctypes.c_int),
     "tflows_cg_noalloc": ([ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_int,
                            ctypes.c_int, ctypes.c_double, _VP, _I, _D, _D], ctypes.c_int),
 }

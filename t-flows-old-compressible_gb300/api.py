@@ -15,6 +15,7 @@ run on torch's current stream.
 from __future__ import annotations
 
 import ctypes
+import os
 from typing import NamedTuple
 
 import numpy as np
@@ -442,3 +443,58 @@ class Assembly:
             self.close()
         except Exception:
             pass
+
+
+def read_mesh(cns_path, geo_path=None):
+    """Load NAME.cns (and NAME.geo) as Process/CnsLoa.f90 and
+    Library/GeoLoa.f90 read them (tflows_mesh_read).  Returns a dict of numpy
+    copies: sizes NC, NbC, NS, NSsh, Nmat; SideC (NS, 3) = SideC(0:2, NS);
+    material, xc, yc, zc over cells -NbC..NC; bcmark, CopyC over -NbC..-1;
+    volume, delta, WallDs over 1..NC; face arrays Sx..zsp over 1..NS."""
+    p = ctypes.POINTER(_native.Mesh)()
+    st = lib().tflows_mesh_read(os.fsencode(cns_path),
+                                os.fsencode(geo_path) if geo_path else None, ctypes.byref(p))
+    if st != OK:
+        raise SolverError(st, last_error())
+    m = p.contents
+    NC, NbC, NS = m.NC, m.NbC, m.NS
+    out = {"NC": NC, "NbC": NbC, "NS": NS, "NSsh": m.NSsh, "Nmat": m.Nmat}
+
+    def take(ptr, n):
+        return np.ctypeslib.as_array(ptr, shape=(max(n, 1),))[:n].copy()
+
+    out["material"] = take(m.material, NbC + NC + 1)
+    out["SideC"] = take(m.SideC, 3 * NS).reshape(NS, 3)
+    out["bcmark"] = take(m.bcmark, NbC)
+    out["CopyC"] = take(m.CopyC, NbC)
+    if geo_path:
+        for k in ("xc", "yc", "zc"):
+            out[k] = take(getattr(m, k), NbC + NC + 1)
+        for k in ("volume", "delta", "WallDs"):
+            out[k] = take(getattr(m, k), NC)
+        for k in ("Sx", "Sy", "Sz", "Dx", "Dy", "Dz", "f", "xsp", "ysp", "zsp"):
+            out[k] = take(getattr(m, k), NS)
+    lib().tflows_mesh_free(p)
+    return out
+
+
+def topolm(NC, SideC):
+    """The solver's compressed-row layout of a face list (tflows_topolm,
+    Process/TopolM.f90:24-98): 1-based (Acol, Arow, Adia, SidAij (NS, 2))
+    with Arow of length NONZ = stored entries + 1."""
+    sc = np.ascontiguousarray(SideC, dtype=np.int32)
+    NS = sc.shape[0]
+    nz = ctypes.c_int()
+    st = lib().tflows_topolm(int(NC), NS, sc.ctypes.data, None, None, None, None,
+                             ctypes.byref(nz))
+    if st != OK:
+        raise SolverError(st, last_error())
+    Acol = np.zeros(NC + 1, np.int32)
+    Arow = np.zeros(nz.value, np.int32)
+    Adia = np.zeros(NC, np.int32)
+    sid = np.zeros((NS, 2), np.int32)
+    st = lib().tflows_topolm(int(NC), NS, sc.ctypes.data, Acol.ctypes.data, Arow.ctypes.data,
+                             Adia.ctypes.data, sid.ctypes.data, ctypes.byref(nz))
+    if st != OK:
+        raise SolverError(st, last_error())
+    return Acol, Arow, Adia, sid

@@ -153,3 +153,53 @@ def test_assembly_rejects_bad_indices():
         tflows.Assembly(d["NC"], d["NbC"], d["NS"], d["NONZ"], bad, d["SidAij"], d["Adia"],
                         d["TypeBC"], {k: d[k] for k in tflows.Assembly.GEOM}, d["volume"])
     assert e.value.status == tflows.BAD_INPUT
+
+
+def test_mesh_files_to_gpu_solve(tmp_path):
+    """A mesh read from T-FlowS files (NAME.cns / NAME.geo), its TopolM
+    layout built by the library, the pressure-correction system assembled on
+    the GPU and solved there: the chain a real T-FlowS case takes."""
+    import torch
+    from fortran_files import write_cns, write_geo
+    m = mesh.box_faces(18, 16, 14, perturb=0.2, seed=6)
+    NC, NbC, NS = m["NC"], m["NbC"], m["NS"]
+    material = np.ones(NbC + NC + 1, np.int32)
+    material[NbC] = 0
+    zeros = np.zeros(NbC, np.int32)
+    faces = {k: m[k] for k in ("Sx", "Sy", "Sz", "Dx", "Dy", "Dz", "f")}
+    for k in ("xsp", "ysp", "zsp"):
+        faces[k] = np.zeros(NS)
+    cns, geo = str(tmp_path / "case.cns"), str(tmp_path / "case.geo")
+    write_cns(cns, NC, NbC, NS, 1, material, m["SideC"], zeros, zeros)
+    write_geo(geo, NbC, m["xc"], m["yc"], m["zc"], m["volume"][NbC + 1:], np.ones(NC),
+              np.ones(NC), faces)
+    r = tflows.read_mesh(cns, geo)
+    Acol, Arow, Adia, sid = tflows.topolm(r["NC"], r["SideC"])
+    vol = np.concatenate([np.zeros(NbC + 1), r["volume"]])
+    tb = np.zeros(NbC + NC + 1, np.int32)
+    tb[:NbC] = 2
+    tb[:NbC:7] = 12  # some pressure boundaries: the matrix is regular
+    asm = tflows.Assembly(NC, NbC, NS, int(Acol[-1]), r["SideC"], sid, Adia, tb,
+                          {k: r[k] for k in tflows.Assembly.GEOM}, vol)
+    rng = np.random.default_rng(3)
+    n = NbC + NC + 1
+    fields = {"asave": _dev(rng.uniform(1.0, 2.0, n))}
+    for k in ("rho_n", "rho_o", "rho_oo"):
+        fields[k] = _dev(rng.uniform(0.5, 1.5, n))
+    for k in ("u", "v", "w", "p", "px", "py", "pz"):
+        fields[k] = _dev(rng.uniform(-1.0, 1.0, n))
+    aval = torch.zeros(int(Acol[-1]), dtype=torch.float64, device="cuda")
+    b = torch.zeros(NC, dtype=torch.float64, device="cuda")
+    abou = torch.zeros(NbC, dtype=torch.float64, device="cuda")
+    flux = torch.zeros(NS, dtype=torch.float64, device="cuda")
+    asm.calcps(fields, aval, b, abou, flux, Nmat=1, dt=0.01)
+    topo = tflows.Topology(NC, Acol - 1, Arow[:-1] - 1, Adia - 1)
+    x = torch.zeros(NC, dtype=torch.float64, device="cuda")
+    tol = 1e-10 * float(b.norm())
+    res = topo.solve(aval[:-1].contiguous(), b, x, "cg", 2, 5000, tol)
+    assert res["status"] == tflows.OK, res
+    import scipy.sparse as sp
+    M = sp.csr_matrix((aval[:-1].cpu().numpy(), Arow[:-1] - 1, Acol - 1), shape=(NC, NC))
+    assert np.linalg.norm(b.cpu().numpy() - M @ x.cpu().numpy()) < 2 * tol
+    asm.close()
+    topo.close()
