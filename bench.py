@@ -240,11 +240,15 @@ def mixed_vs_fp64(pkg, dev, scale, precs, reps):
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
 
     def run(prec, opts):
+        # every variant runs with its own tuned launch shape (tuned on the
+        # first, untimed solve)
+        opts.autotune = 1
         el, out = device_solves(pkg, topo, val, b, x, "cg", prec, s.tol, opts, reps, 1)
         r = out[-1]
         return {"ms": 1e3 * el / reps, "iterations": r["iterations"],
                 "refinements": r["refinements"], "fin_res": r["fin_res"],
-                "gbs": r["bytes"] / r["seconds"] / 1e9, "status": r["status"]}, x.clone()
+                "gbs": r["bytes"] / r["seconds"] / 1e9, "status": r["status"],
+                "block_size": r["block_size"], "grid_blocks": r["grid_blocks"]}, x.clone()
 
     result = {}
     for prec in precs:
@@ -542,6 +546,9 @@ def main():
                     help="edge of the cfg3 mixed-vs-FP64 comparison (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (cfg4) block")
+    ap.add_argument("--ic-sweeps", type=int, default=0,
+                    help="mixed + prec 2: Jacobi sweeps per triangle (0 = exact sweeps)")
+    ap.add_argument("--ic-bf16", action="store_true", help="mixed + prec 2: BF16 factor entries")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the config-2 method, config-5 adjoint and SIMPLE-step blocks")
     ap.add_argument("--no-autotune", action="store_true",
@@ -576,12 +583,13 @@ def main():
     b = torch.from_numpy(s.b.copy()).to(dev)
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
     prec_mode = {"fp64": pkg.FP64, "fp64_fma": pkg.FP64_FMA, "mixed": pkg.MIXED}[args.precision]
-    opts = pkg.options(precision=prec_mode, autotune=int(not args.no_autotune))
+    ic = {"ic_sweeps": args.ic_sweeps, "ic_bf16": int(args.ic_bf16)}
+    opts = pkg.options(precision=prec_mode, autotune=int(not args.no_autotune), **ic)
     tuning = None
     if not args.no_autotune:
         # launch shape (threads per block, rows per warp) timed on this
         # system before the timed region; every timed solve uses it
-        tuning = topo.autotune(val, b, method, prec, opts=pkg.options(precision=prec_mode))
+        tuning = topo.autotune(val, b, method, prec, opts=pkg.options(precision=prec_mode, **ic))
 
     def barrier():
         if world > 1:

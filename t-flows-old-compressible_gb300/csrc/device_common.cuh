@@ -230,31 +230,6 @@ __device__ __forceinline__ void grid_init(Grid& g, DevCtl* ctl, double* partials
     grid_init_group(g, ctl, partials, timeout_cyc, 0, gridDim.x);
 }
 
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Wait (one thread) until *p >= target; bounded like every other wait.
-__device__ __forceinline__ bool wait_count(const unsigned* p, unsigned target, DevCtl* ctl,
-                                           long long timeout_cyc, int where) {
-    if (ld_acquire_u32(p) >= target) return true;
-    long long t0 = clock64();
-    unsigned spins = 0;
-    while (true) {
-        __nanosleep(32);
-        if (ld_acquire_u32(p) >= target) return true;
-        if ((++spins & 127u) == 0u) {
-            if (ld_relaxed_s32(&ctl->abort)) return false;
-            if (clock64() - t0 > timeout_cyc) {
-                raise_abort(ctl, ST_TIMEOUT, where);
-                return false;
-            }
-        }
-    }
-}
-
 // Grid-wide barrier with release/acquire ordering (every write before the
 // barrier is visible to every read after it).  Returns false when the
 // launch was aborted (timeout or error raised anywhere).
