@@ -60,6 +60,7 @@ struct Mat {
     int wide_f;  // chunks in the widest forward / backward level
     int wide_b;
     int sweep_mult;  // sweep warps per chunk of the widest level (0 = default)
+    int sweep_sleep; // longest pause between polls of a sweep cell, ns (0: none)
 };
 
 template <typename T>
@@ -246,9 +247,6 @@ __device__ __forceinline__ T diag_value(const Mat<T>& m, int i) {
 constexpr int kSweepMax = 8;  // dependencies prefetched per row
 // Longest pause between polls of not-yet-ready cells, in ns (0: poll back to
 // back).
-#ifndef TFLOWS_SWEEP_SLEEP
-#define TFLOWS_SWEEP_SLEEP 512
-#endif
 // Warps taking part in a sweep: at most `per_chunk` (a tuning parameter,
 // default 4) per chunk of the widest level, so that a warp's next chunk is
 // only a few levels ahead of the front and its polls rarely spin long.
@@ -329,10 +327,10 @@ __device__ __forceinline__ bool sweep_chunk(const Grid& g, const Mat<T>& m, int 
         }
         if (__all_sync(0xffffffffu, done)) return true;
         // back off while the inputs are far from ready (a chunk several
-        // levels ahead of the front), never more than TFLOWS_SWEEP_SLEEP ns
+        // levels ahead of the front), never more than m.sweep_sleep ns
         ++spins;
-        if (TFLOWS_SWEEP_SLEEP > 0 && spins > 4u)
-            __nanosleep(min((unsigned)TFLOWS_SWEEP_SLEEP, 8u << min(spins - 4u, 10u)));
+        if (m.sweep_sleep > 0 && spins > 4u)
+            __nanosleep(min((unsigned)m.sweep_sleep, 8u << min(spins - 4u, 10u)));
         if ((spins & 63u) == 0u) {
             bool quit = ld_relaxed_s32(&g.ctl->abort) != 0;
             if (!quit && clock64() - start > g.timeout_cyc) {
