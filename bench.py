@@ -173,6 +173,7 @@ def run_reference(args):
         "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(s, "bicg", 1),
+        "arithmetic": "FP64 as the reference (oracle C restatement, no fused multiply-adds)",
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
                          "sample": f"{cores} concurrent full BiCG solves per step "
                                    f"({it} iterations each), oracle C restatement, 1 thread each"},
@@ -182,11 +183,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def workload_config(s, method, prec, precision="fp64"):
-    return {"workload": f"{s.name}: BiCG/CG solve to 1e-8*||b|| (absolute test as the reference), "
-                        f"x0=0, {method}, prec {prec}, {precision}",
-            "n": s.N, "nnz": s.nnz, "method": method, "prec": prec, "precision": precision,
+def workload_config(s, method, prec):
+    return {"workload": f"{s.name}: {method} solve to 1e-8*||b|| (absolute test as the "
+                        f"reference), x0=0, prec {prec}",
+            "n": s.N, "nnz": s.nnz, "method": method, "prec": prec,
             "l2": "inputs larger than L2 (no flush)"}
+
+
+ARITHMETIC = {"fp64": "FP64, reference arithmetic (separate rounded products and sums)",
+              "fp64_fma": "FP64 with fused multiply-adds and a reciprocal diagonal",
+              "mixed": "FP32 inner solves, FP64 refinement"}
 
 
 def make_workload(pkg, name, scale):
@@ -615,9 +621,10 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if args.precision == "mixed" else "f64",
         "data": "synthetic",
-        "config": dict(workload_config(s, method, prec, args.precision),
-                       launch=({"autotuned": True, **tuning} if tuning else
-                               {"autotuned": False, "block_size": 256})),
+        "config": workload_config(s, method, prec),
+        "arithmetic": ARITHMETIC[args.precision],
+        "launch": ({"autotuned": True, **tuning} if tuning else
+                   {"autotuned": False, "block_size": 256}),
         "iterations": int(statistics.median(iters)),
         "time_to_tol_ms": 1e3 * el / args.steps,
     }
