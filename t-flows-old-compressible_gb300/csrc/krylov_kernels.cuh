@@ -188,6 +188,49 @@ __device__ __forceinline__ T sell_row(const Mat<T>& m, int s, int lane, const X*
     return acc;
 }
 
+// q_i = sum_j a_ij (z_j + beta p_j): the product with the next search
+// direction formed inside the gather (FP32 inner solves), so the update
+// p = z + beta p needs no pass of its own and no grid barrier.  `first`:
+// p = z.  The direction is formed with one fused multiply-add, exactly as
+// the row's owner forms its own entry (fused_dir), so every product sees the
+// same vector the iteration stores.
+__device__ __forceinline__ float fused_dir(float z, float beta, float p, bool first) {
+    return first ? z : __fmaf_rn(beta, p, z);
+}
+
+__device__ __forceinline__ float sell_row_dir(const Mat<float>& m, int s, int lane,
+                                              const float* __restrict__ z,
+                                              const float* __restrict__ p, float beta, bool first) {
+    const long long b0 = m.soff[s];
+    const int w = (int)((m.soff[s + 1] - b0) >> 5);
+    const int* cp = m.scol + b0 + lane;
+    const float* vp = m.sval + b0 + lane;
+    float acc = 0.f;
+    if (w <= 8) {
+        int c[8];
+        float v[8], zz[8], pp[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            c[t] = t < w ? cp[32 * t] : -1;
+            v[t] = t < w ? vp[32 * t] : 0.f;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            zz[t] = c[t] >= 0 ? z[c[t]] : 0.f;
+            pp[t] = c[t] >= 0 && !first ? p[c[t]] : 0.f;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (c[t] >= 0) acc = acc + v[t] * fused_dir(zz[t], beta, pp[t], first);
+        return acc;
+    }
+    for (int t = 0; t < w; ++t) {
+        const int c = cp[32 * t];
+        if (c >= 0) acc = acc + vp[32 * t] * fused_dir(z[c], beta, first ? 0.f : p[c], first);
+    }
+    return acc;
+}
+
 // r_i <- r_i - a_i1 x_1 - a_i2 x_2 - ... (Process/Resid.f90:28-33 order).
 template <typename T, typename X>
 __device__ __forceinline__ T sell_resid_row(const Mat<T>& m, int s, int lane, T ri,
@@ -596,6 +639,9 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
     double rho = 0.0, rhoold = 0.0;
     bool nonfinite = false;
     int iter = 1;
+    // search direction; the FP32 inner solves alternate between p and t
+    T* pcur = v.p;
+    T* pnext = v.t;
     for (; iter <= cfg.maxiter; ++iter) {
         if (prec == 2) {
             T a[1] = {T(0)};
@@ -611,6 +657,36 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         } else {
             rho = rho_next;
         }
+        bool fused = false;
+        if constexpr (sizeof(T) == 4) {
+            if (prec != 2) {
+                // FP32 inner solves, diagonal or no preconditioning: the new
+                // search direction goes into the other p buffer as the
+                // product forms it (no separate update pass, one barrier
+                // less per iteration)
+                const float beta = iter == 1 ? 0.f : float(rho / rhoold);
+                const bool first = iter == 1;
+                const float* pold = pcur;
+                float* pnew = pnext;
+                float a1[1] = {0.f};
+                for (int s = g.wg; s < m.nslices; s += g.nw) {
+                    const int i = s * kWarp + g.lane;
+                    const float qi = sell_row_dir(m, s, g.lane, z, pold, beta, first);
+                    if (i < m.n) {
+                        const float pi = fused_dir(z[i], beta, first ? 0.f : pold[i], first);
+                        pnew[i] = pi;
+                        v.q[i] = qi;
+                        a1[0] += pi * qi;
+                    }
+                }
+                pcur = pnew;
+                pnext = const_cast<float*>(pold);
+                publish_t<1>(g, SLOT_C, a1);
+                if (!grid_sync(g, 43)) { out.exit_kind = EXIT_ABORT; return; }
+                fused = true;
+            }
+        }
+        if (!fused) {
         // p = z + beta p  (CG.f90:178-187)
         if (iter == 1) {
             TF_FOR4(g, m, i) { st4(v.p + i, ld4(z + i)); }
@@ -637,6 +713,7 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         }
         publish_t<1>(g, SLOT_C, a1);
         if (!grid_sync(g, 43)) { out.exit_kind = EXIT_ABORT; return; }
+        }
         double t1[1];
         totals<1>(g, SLOT_C, t1);
         const double alfa_d = rho / t1[0];
@@ -645,7 +722,7 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         T a3[3] = {T(0), T(0), T(0)};
         TF_FOR4(g, m, i) {
             V4<T> xx = ld4(v.x + i), rr = ld4(v.r + i);
-            const V4<T> pp = ld4(v.p + i), qq = ld4(v.q + i);
+            const V4<T> pp = ld4(pcur + i), qq = ld4(v.q + i);
             V4<T> dd, zz;
             if (prec == 1) dd = ld4(v.D + i);
 #pragma unroll
