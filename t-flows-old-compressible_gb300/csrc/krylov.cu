@@ -416,11 +416,11 @@ double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevSta
     if (rq.precision == 1) {
         const double spmv32 = (double)t.nnz * 8.0 + sl + 8.0 * t.n;
         const double ic = rq.prec == 2 ? ic_bytes(rq.ic_bf16 ? 2.0 : 4.0, 4.0) : 0.0;
-        // restarted CG with diagonal or no preconditioning forms its search
-        // direction inside the product (z and p read once, p and q written once), so
+        // restarted CG forms its search direction inside the product (z and
+        // p read once, p and q written once), so
         // the product's own vector read and write are part of the 4·N·12
         // (resp. 10) vector bytes
-        const double cg_fused = (rq.prec == 2 || !rq.refine_restart) ? 8.0 * t.n : 0.0;
+        const double cg_fused = !rq.refine_restart ? 8.0 * t.n : 0.0;
         const double inner_it = cgs ? 2 * spmv32 + 4.0 * t.n * 22 + 2 * ic
                                     : spmv32 - 8.0 * t.n + cg_fused +
                                           4.0 * t.n * (rq.prec == 1 ? 12 : 10) + ic;

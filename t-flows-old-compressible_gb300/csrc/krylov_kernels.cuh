@@ -659,11 +659,10 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         }
         bool fused = false;
         if constexpr (sizeof(T) == 4) {
-            if (prec != 2) {
-                // FP32 inner solves, diagonal or no preconditioning: the new
-                // search direction goes into the other p buffer as the
-                // product forms it (no separate update pass, one barrier
-                // less per iteration)
+            {
+                // FP32 inner solves: the new search direction goes into the
+                // other p buffer as the product forms it (no separate update
+                // pass, one barrier less per iteration)
                 const float beta = iter == 1 ? 0.f : float(rho / rhoold);
                 const bool first = iter == 1;
                 const float* pold = pcur;
