@@ -284,7 +284,10 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
     """48 independent systems of uneven size (log-uniform 16^3..160^3 cells),
     odd ones variable-density pressure (CG + IC), even ones scalar transport
     (BiCG + diagonal), mixed precision with FP64 refinement to 1e-8 relative,
-    solved by one graph-captured persistent launch per replay."""
+    solved by one graph-captured persistent launch per replay.  The IC(0)
+    systems run with BF16 factor entries and either exact triangular sweeps
+    or one Jacobi sweep per triangle; the faster plan is the block's result,
+    both are reported."""
     import torch
     shapes = pkg.mesh.batch_sizes(count)
     systems = []
@@ -299,36 +302,47 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
     vals = [torch.from_numpy(s.A[:-1].copy()).to(dev) for s, _, _ in systems]
     bs = [torch.from_numpy(s.b.copy()).to(dev) for s, _, _ in systems]
     xs = [torch.zeros(s.N, dtype=torch.float64, device=dev) for s, _, _ in systems]
-    opts = pkg.options(precision=pkg.MIXED, tol_mode=pkg.TOL_RELATIVE, autotune=int(autotune))
-    plan = pkg.Plan(topos, vals, bs, xs, [m for _, m, _ in systems], [p for _, _, p in systems],
-                    [20000] * count, [1e-8] * count, opts)
-    tuning = plan.tuning()
-    plan.launch()
-    res = plan.results()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(reps):
-        for x in xs:
-            x.zero_()
-        plan.launch()
-    e1.record()
-    res = plan.results()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
     rows = sum(s.N for s, _, _ in systems)
-    byts = sum(r["bytes"] for r in res)
-    ok = sum(1 for r in res if r["status"] == pkg.OK)
-    plan.close()
-    return {"workload": f"{count} systems, sizes {min(s.N for s, _, _ in systems)}.."
-                        f"{max(s.N for s, _, _ in systems)} rows (total {rows}), odd: CG+IC "
-                        "pressure, even: BiCG+diag transport, mixed precision, tol 1e-8 relative, "
-                        "one graph-captured cooperative launch",
-            "ms_per_batch": ms, "systems_per_s": count * 1e3 / ms, "converged": ok,
-            "tuning": tuning,
-            "group_blocks": [r["grid_blocks"] for r in res],
+    variants = {}
+    for label, ic in (("ic_exact_bf16", {"ic_bf16": 1}),
+                      ("ic_jacobi1_bf16", {"ic_bf16": 1, "ic_sweeps": 1})):
+        opts = pkg.options(precision=pkg.MIXED, tol_mode=pkg.TOL_RELATIVE,
+                           autotune=int(autotune), **ic)
+        for x in xs:
+            x.zero_()  # the plan tunes on x0 = 0, as every replay starts
+        plan = pkg.Plan(topos, vals, bs, xs, [m for _, m, _ in systems],
+                        [p for _, _, p in systems], [20000] * count, [1e-8] * count, opts)
+        tuning = plan.tuning()
+        plan.launch()
+        plan.results()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            for x in xs:
+                x.zero_()
+            plan.launch()
+        e1.record()
+        res = plan.results()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        byts = sum(r["bytes"] for r in res)
+        variants[label] = {
+            "ms_per_batch": ms, "systems_per_s": count * 1e3 / ms,
+            "converged": sum(1 for r in res if r["status"] == pkg.OK),
             "max_iterations": max(r["iterations"] for r in res),
-            "gbs": byts / (ms * 1e-3) / 1e9}
+            "gbs": byts / (ms * 1e-3) / 1e9, "tuning": tuning,
+            "group_blocks": [r["grid_blocks"] for r in res]}
+        plan.close()
+    best = min(variants, key=lambda k: variants[k]["ms_per_batch"])
+    out = {"workload": f"{count} systems, sizes {min(s.N for s, _, _ in systems)}.."
+                       f"{max(s.N for s, _, _ in systems)} rows (total {rows}), odd: CG+IC "
+                       "pressure, even: BiCG+diag transport, mixed precision, tol 1e-8 relative, "
+                       "one graph-captured cooperative launch",
+           "variant": best, **variants[best]}
+    out["all_variants"] = {k: {kk: vv for kk, vv in v.items() if kk != "group_blocks"}
+                           for k, v in variants.items()}
+    return out
 
 
 def cfg2_methods(pkg, dev, topo, s, val, b, reps=3):
