@@ -244,7 +244,9 @@ int tflows_autotune(tflows_topology *topo, int method, int prec,
  * TFLOWS_TUNE_FILE table again (the file is left as it is). */
 void tflows_autotune_clear(void);
 /* The batched-launch tuning a plan made at creation (options.autotune = 1:
- * block size and group sizes from timed full solves). */
+ * block size and group sizes from timed full solves, each starting from the
+ * contents of vals/bs/xs at creation -- give the plan the kind of initial
+ * guesses its replays will use, not converged solutions). */
 int tflows_plan_tuning(const tflows_plan *plan, tflows_batch_tuning *out);
 
 /* grad_val[k] = -lambda[row(k)] * x[col(k)] over the stored pattern: the
