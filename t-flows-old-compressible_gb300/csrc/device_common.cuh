@@ -123,39 +123,6 @@ template <> struct Cell<float> {
     __device__ static __forceinline__ float sentinel() { return __int_as_float(kSentinel); }
 };
 
-// Wait until *p holds a produced value.  Bounded: gives up after
-// `timeout_cyc` of waiting or when another thread raised the abort flag;
-// then returns false (the caller must stop its phase).
-template <typename T>
-__device__ __forceinline__ bool wait_cell(const T* p, T& out, DevCtl* ctl, long long timeout_cyc,
-                                          int where) {
-    using C = Cell<T>;
-    auto b = C::load(p);
-    if (b != C::kSentinel) {
-        out = C::value(b);
-        return true;
-    }
-    long long t0 = clock64();
-    unsigned spins = 0;
-    while (true) {
-        // exponential back-off 32 -> 512 ns keeps many waiting threads from
-        // flooding L2 with polls
-        __nanosleep(32u << (spins < 4u ? spins : 4u));
-        b = C::load(p);
-        if (b != C::kSentinel) {
-            out = C::value(b);
-            return true;
-        }
-        if ((++spins & 63u) == 0u) {
-            if (ld_relaxed_s32(&ctl->abort)) return false;
-            if (clock64() - t0 > timeout_cyc) {
-                raise_abort(ctl, ST_TIMEOUT, where);
-                return false;
-            }
-        }
-    }
-}
-
 // ---- reductions ---------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
