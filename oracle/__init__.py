@@ -2,8 +2,8 @@
 
 ctypes access to the C restatement of the reference's Krylov solver path.
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline and
-reference legs import this package, as the checker or the timed CPU
-baseline; the product library never loads it.
+reference legs import this package, as the reference the GPU results are
+compared with or as the timed CPU baseline; the product library never loads it.
 """
 from __future__ import annotations
 

@@ -7,8 +7,8 @@
  * (including the outer `do m = 1, Nmat` loops, which repeat the face loop
  * and the source loop Nmat times) and left-to-right evaluation of every
  * expression follow the source; compiled with -ffp-contract=off like the
- * solver restatement.  Only tests/ use it, as the checker of the GPU
- * assembly kernels.
+ * solver restatement.  Only tests/ use it, to compare the GPU assembly
+ * kernels against.
  *
  * Parity pin: tests/golden/assembly_*.npz hold the outputs of the reference's
  * own source text of those lines executed statement by statement

@@ -1,8 +1,8 @@
 /*
  * ORACLE -- TEST INFRASTRUCTURE ONLY.  Nothing in the product path links,
  * loads or calls this file; only tests/, __graft_entry__.smoke() and the
- * cpu_baseline / reference legs of bench.py use it, always as the checker or
- * as the timed CPU baseline, never as the thing measured or shipped.
+ * cpu_baseline / reference legs of bench.py use it, always as the reference
+ * results are compared with or as the timed CPU baseline, never as the thing measured or shipped.
  *
  * A plain-C, statement-by-statement restatement of the Krylov linear-solver
  * path of T-FlowS (FP64, Fortran REAL with -fdefault-real-8):
