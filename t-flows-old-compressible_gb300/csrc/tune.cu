@@ -45,13 +45,20 @@ Table& table() {
     return *t;
 }
 
+// Device name and SM count, looked up once per device (the property query is
+// far too slow to repeat on every solve that consults the table).
 std::string device_tag(int device) {
+    static std::mutex mu;
+    static std::map<int, std::string> tags;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = tags.find(device);
+    if (it != tags.end()) return it->second;
     cudaDeviceProp p;
     if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return "unknown";
     std::string name = p.name;
     for (char& c : name)
         if (c == ' ') c = '_';
-    return name + "/" + std::to_string(p.multiProcessorCount);
+    return tags[device] = name + "/" + std::to_string(p.multiProcessorCount);
 }
 
 // Size class: quarter octaves of the row count, half entries per row.
