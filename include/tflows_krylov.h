@@ -85,6 +85,10 @@ typedef struct tflows_options {
     int rows_per_warp;   /* rows each warp owns, sets the grid (0 = 32)     */
     int sweep_warps;     /* IC sweeps: warps per chunk of the widest
                             wavefront level (0 = 4)                         */
+    int sweep_gate;      /* IC sweeps: 1 = a waiting warp polls one
+                            representative cell until it is ready, 0 = every
+                            lane polls every input, -1 = the default (on,
+                            TFLOWS_SWEEP_GATE=0 turns it off)              */
 } tflows_options;
 
 typedef struct tflows_result {
@@ -111,6 +115,7 @@ typedef struct tflows_tuning {
     int from_table;      /* 1 = the table already held this class           */
     double us_per_iteration;         /* chosen shape                        */
     double default_us_per_iteration; /* 256 threads, one slice per warp     */
+    int sweep_gate;      /* IC sweeps: gated polling chosen (-1 = default)  */
 } tflows_tuning;
 
 /* Batched-launch tuning of a plan: block size and block-group balance. */

@@ -99,7 +99,7 @@ class Options(ctypes.Structure):
                 ("block_size", ctypes.c_int), ("grid_blocks", ctypes.c_int),
                 ("device", ctypes.c_int), ("inject_stall", ctypes.c_int),
                 ("autotune", ctypes.c_int), ("rows_per_warp", ctypes.c_int),
-                ("sweep_warps", ctypes.c_int)]
+                ("sweep_warps", ctypes.c_int), ("sweep_gate", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -119,7 +119,7 @@ class Tuning(ctypes.Structure):
                 ("grid_blocks", ctypes.c_int), ("sweep_warps", ctypes.c_int),
                 ("candidates", ctypes.c_int), ("from_table", ctypes.c_int),
                 ("us_per_iteration", ctypes.c_double),
-                ("default_us_per_iteration", ctypes.c_double)]
+                ("default_us_per_iteration", ctypes.c_double), ("sweep_gate", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

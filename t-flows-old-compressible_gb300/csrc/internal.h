@@ -79,6 +79,7 @@ struct SolveRequest {
     int grid = 0;           // persistent blocks (0 = from rows_per_warp)
     int rows_per_warp = 0;  // rows each warp owns (0 = one 32-row slice)
     int sweep_mult = 0;     // IC sweep warps per chunk of the widest level (0 = 4)
+    int sweep_gate = -1;    // IC sweeps: gated polling 1 / 0, -1 = process default
     int autotune = 0;       // take block/rows_per_warp/sweep_mult from the tuner
 };
 
@@ -164,6 +165,7 @@ struct TuneChoice {
     int rows_per_warp = 0;
     int grid = 0;
     int sweep_mult = 0;
+    int sweep_gate = -1;
     int candidates = 0;
     int from_cache = 0;
     double us_per_iter = 0.0;

@@ -129,6 +129,15 @@ int sweep_sleep_ns() {
     return v;
 }
 
+// Gated polling in the IC sweeps (TFLOWS_SWEEP_GATE=0 turns it off).
+int sweep_gate_on() {
+    static const int v = [] {
+        const char* e = std::getenv("TFLOWS_SWEEP_GATE");
+        return e && *e ? (std::atoi(e) != 0) : 1;
+    }();
+    return v;
+}
+
 template <typename T>
 Mat<T> make_mat(const DeviceTopology& t, const T* sval) {
     Mat<T> m;
@@ -147,6 +156,7 @@ Mat<T> make_mat(const DeviceTopology& t, const T* sval) {
     m.wide_b = t.wide_b;
     m.sweep_mult = 0;
     m.sweep_sleep = sweep_sleep_ns();
+    m.sweep_gate = sweep_gate_on();
     return m;
 }
 
@@ -332,6 +342,7 @@ cudaError_t prepare_fp64(const DeviceTopology& t, Workspace& ws, const SolveRequ
     std::memset(&P, 0, sizeof(P));
     P.m = make_mat<double>(t, ws.sval64);
     P.m.sweep_mult = rq.sweep_mult;
+    if (rq.sweep_gate >= 0) P.m.sweep_gate = rq.sweep_gate;
     P.v = carve<double>(ws.vec64, ws.vec_cap, x, r);
     P.cfg.method = rq.method == 2 || rq.method == 3 ? rq.method : 0;
     if (rq.method == 3) P.mT = make_mat<double>(t, ws.svalT64);
@@ -365,6 +376,7 @@ cudaError_t prepare_mixed(const DeviceTopology& t, Workspace& ws, const SolveReq
     P.m32 = make_mat<float>(t, ws.sval32);
     P.m64.sweep_mult = rq.sweep_mult;
     P.m32.sweep_mult = rq.sweep_mult;
+    if (rq.sweep_gate >= 0) P.m64.sweep_gate = P.m32.sweep_gate = rq.sweep_gate;
     P.x64 = x;
     P.r64 = r;
     double* b64 = ws.vec64 + 13 * ws.vec_cap;

@@ -61,6 +61,7 @@ struct Mat {
     int wide_b;
     int sweep_mult;  // sweep warps per chunk of the widest level (0 = default)
     int sweep_sleep; // longest pause between polls of a sweep cell, ns (0: none)
+    int sweep_gate;  // 1: a waiting warp polls one representative cell first
 };
 
 template <typename T>
@@ -330,10 +331,31 @@ __device__ __forceinline__ bool sweep_chunk(const Grid& g, const Mat<T>& m, int 
     }
     int cursor = t0;
     bool done = row < 0;
+    // Gate: while the chunk's inputs are far from ready, one lane polls one
+    // representative cell (its dependency nearest in row order: the last
+    // lower entry forward, the first upper entry backward) instead of every
+    // lane polling every cell; the whole warp polls once it is in.  This
+    // keeps thousands of early warps from loading L2 with polls.
+    int gate_lane = -1, gate_col = 0;
+    if (m.sweep_gate) {
+        int rc = 0;
+#pragma unroll
+        for (int u = 0; u < kSweepMax; ++u)
+            if (KIND == 1 ? u == 0 : u == n - 1) rc = c[u];
+        const unsigned has = __ballot_sync(0xffffffffu, !longrow && n > 0);
+        gate_lane = has ? __ffs(has) - 1 : -1;
+        gate_col = __shfl_sync(0xffffffffu, rc, gate_lane < 0 ? 0 : gate_lane);
+    }
+    bool gated = gate_lane >= 0;
     const long long start = clock64();
     unsigned spins = 0;
     while (true) {
-        if (!done) {
+        if (gated) {
+            int ready = 0;
+            if (g.lane == gate_lane) ready = C::load(cells + gate_col) != C::kSentinel;
+            gated = !__shfl_sync(0xffffffffu, ready, gate_lane);
+        }
+        if (!done && !gated) {
             if (longrow) {
                 while (cursor < t1) {
                     const auto b = C::load(cells + m.scol[base + 32LL * cursor]);

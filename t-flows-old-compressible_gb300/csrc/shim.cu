@@ -78,6 +78,7 @@ void default_opts(tflows_options* o) {
     o->autotune = 0;
     o->rows_per_warp = 0;
     o->sweep_warps = 0;
+    o->sweep_gate = -1;
     o->device = -1;
 }
 
@@ -379,6 +380,7 @@ SolveRequest make_request(const tflows_options& o, int method, int prec, int max
     rq.grid = o.grid_blocks;
     rq.rows_per_warp = o.rows_per_warp;
     rq.sweep_mult = o.sweep_warps;
+    rq.sweep_gate = o.sweep_gate < 0 ? -1 : (o.sweep_gate != 0);
     rq.autotune = o.autotune && o.block_size == 0 && o.grid_blocks == 0 ? 1 : 0;
     return rq;
 }
@@ -1086,6 +1088,7 @@ int tflows_autotune(tflows_topology* topo, int method, int prec, const tflows_op
     out->rows_per_warp = ch.rows_per_warp;
     out->grid_blocks = planned_grid(topo->t, rq);
     out->sweep_warps = ch.sweep_mult;
+    out->sweep_gate = ch.sweep_gate;
     out->candidates = ch.candidates;
     out->from_table = ch.from_cache;
     out->us_per_iteration = ch.us_per_iter;

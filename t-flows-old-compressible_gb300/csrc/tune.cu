@@ -78,7 +78,7 @@ const char* table_path() {
 }
 
 // One line per entry: the key fields, then block rows_per_warp sweep_mult
-// and the measured microseconds per iteration.
+// sweep_gate and the measured microseconds per iteration.
 void load_file(Table& T) {
     T.loaded = true;
     const char* path = table_path();
@@ -86,14 +86,15 @@ void load_file(Table& T) {
     FILE* f = std::fopen(path, "r");
     if (!f) return;
     char dev[256];
-    int a, b, c, d, e, g, h, i, blk, rpw, sm;
+    int a, b, c, d, e, g, h, i, blk, rpw, sm, gate;
     double us;
-    while (std::fscanf(f, "%255s %d %d %d %d %d %d %d %d %d %d %d %lf", dev, &a, &b, &c, &d, &e,
-                       &g, &h, &i, &blk, &rpw, &sm, &us) == 13) {
+    while (std::fscanf(f, "%255s %d %d %d %d %d %d %d %d %d %d %d %d %lf", dev, &a, &b, &c, &d,
+                       &e, &g, &h, &i, &blk, &rpw, &sm, &gate, &us) == 14) {
         TuneChoice ch;
         ch.block = blk;
         ch.rows_per_warp = rpw;
         ch.sweep_mult = sm;
+        ch.sweep_gate = gate;
         ch.us_per_iter = us;
         T.entries[Key(dev, a, b, c, d, e, g, h, i)] = ch;
     }
@@ -105,22 +106,23 @@ void append_file(const Key& k, const TuneChoice& ch) {
     if (!path) return;
     FILE* f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "%s %d %d %d %d %d %d %d %d %d %d %d %.6g\n", std::get<0>(k).c_str(),
+    std::fprintf(f, "%s %d %d %d %d %d %d %d %d %d %d %d %d %.6g\n", std::get<0>(k).c_str(),
                  std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k), std::get<5>(k),
                  std::get<6>(k), std::get<7>(k), std::get<8>(k), ch.block, ch.rows_per_warp,
-                 ch.sweep_mult, ch.us_per_iter);
+                 ch.sweep_mult, ch.sweep_gate, ch.us_per_iter);
     std::fclose(f);
 }
 
 // Microseconds per iteration of one capped solve from x0 = 0 (best of two).
 int time_shape(const DeviceTopology& t, Workspace& ws, const SolveRequest& base, const double* b,
-               int block, int rpw, int sweep_mult, cudaStream_t s, double& us, int& grid,
-               std::string& msg) {
+               int block, int rpw, int sweep_mult, int sweep_gate, cudaStream_t s, double& us,
+               int& grid, std::string& msg) {
     SolveRequest rq = base;
     rq.block = block;
     rq.rows_per_warp = rpw;
     rq.grid = 0;
     rq.sweep_mult = sweep_mult;
+    rq.sweep_gate = sweep_gate;
     rq.tol = 1e-30;  // relative: never reached within the cap
     rq.tol_relative = 1;
     rq.x_is_zero = 1;
@@ -167,6 +169,7 @@ void tune_apply(const TuneChoice& ch, SolveRequest& rq) {
     rq.block = ch.block;
     rq.rows_per_warp = ch.rows_per_warp;
     rq.sweep_mult = ch.sweep_mult;
+    rq.sweep_gate = ch.sweep_gate;
     rq.grid = 0;
 }
 
@@ -192,7 +195,7 @@ int tune_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, c
             seen.emplace_back(blk, want);
             double us = 0.0;
             int grid = 0;
-            const int st = time_shape(t, ws, rq, b, blk, rpw, 0, s, us, grid, msg);
+            const int st = time_shape(t, ws, rq, b, blk, rpw, 0, rq.sweep_gate, s, us, grid, msg);
             if (st != TFLOWS_OK) return st;
             ++count;
             if (blk == 256 && rpw == 0) out.default_us_per_iter = us;
@@ -207,11 +210,26 @@ int tune_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, c
         for (int sm : {2, 8}) {
             double us = 0.0;
             int grid = 0;
-            const int st = time_shape(t, ws, rq, b, best.block, best.rows_per_warp, sm, s, us, grid, msg);
+            const int st = time_shape(t, ws, rq, b, best.block, best.rows_per_warp, sm,
+                                      rq.sweep_gate, s, us, grid, msg);
             if (st != TFLOWS_OK) return st;
             ++count;
             if (us < best.us_per_iter) {
                 best.sweep_mult = sm;
+                best.us_per_iter = us;
+            }
+        }
+        // gated polling on and off (it pays on large systems, where
+        // thousands of warps wait)
+        for (int gate : {0, 1}) {
+            double us = 0.0;
+            int grid = 0;
+            const int st = time_shape(t, ws, rq, b, best.block, best.rows_per_warp,
+                                      best.sweep_mult, gate, s, us, grid, msg);
+            if (st != TFLOWS_OK) return st;
+            ++count;
+            if (us < best.us_per_iter) {
+                best.sweep_gate = gate;
                 best.us_per_iter = us;
             }
         }
