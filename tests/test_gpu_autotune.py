@@ -139,3 +139,18 @@ def test_autotuned_plan_balances_groups_and_keeps_answers():
     plan.close()
     for t in topos:
         t.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_gated_polling_changes_no_bit(precision):
+    """Gated polling only changes when a warp looks at its inputs, not what
+    it computes: with the same launch shape the solution is bit-identical."""
+    s = mesh.pressure_system(24, 20, 18, perturb=0.2, seed=4, variable_density=True)
+    topo = tflows.Topology.from_system(s)
+    xs = []
+    for gate in (0, 1):
+        x, r = _solve(topo, s, "cg", 2, precision=precision, sweep_gate=gate)
+        assert r["status"] == tflows.OK
+        xs.append(x)
+    assert np.array_equal(xs[0].view(np.uint64), xs[1].view(np.uint64))
+    topo.close()
