@@ -25,7 +25,7 @@ _I = ctypes.POINTER(ctypes.c_int)
 
 def build(force: bool = False) -> str:
     """Compile the oracle with make (gcc, -O3 -ffp-contract=off)."""
-    srcs = ("krylov_oracle.c", "assembly_oracle.c")
+    srcs = ("krylov_oracle.c", "assembly_oracle.c", "momentum_oracle.c")
     if force or not os.path.exists(LIB_PATH) or any(
             os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, f)) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
@@ -58,6 +58,11 @@ def lib():
             L.oracle_calcps_assembly.argtypes = (
                 [ctypes.c_int] * 5 + [ctypes.c_double] + [_I] * 4 + [_D] * 24)
             L.oracle_calcps_assembly.restype = None
+            _PP = ctypes.POINTER(_D)
+            L.oracle_newuvw_assembly.argtypes = (
+                [ctypes.c_int] * 4 + [_I, _D] + [_I] * 7 + [_D] * 3 + [_PP] * 3 + [_D] * 5
+                + [_I])
+            L.oracle_newuvw_assembly.restype = None
             _lib = L
     return _lib
 
@@ -165,3 +170,47 @@ def calcps_assembly(NC, NbC, NS, NONZ, Nmat, dt, SideC, SidAij, Adia, TypeBC, ge
                                  *[_dp(a) for a in fl], _dp(Aval), _dp(b), _dp(Abou), _dp(Flux),
                                  ctypes.byref(em))
     return Aval, b, Abou[:NbC], Flux, em.value
+
+
+MOMENTUM_CELL_FIELDS = ("rho_n", "rho_o", "rho_oo", "ui_n", "ui_o", "ui_oo", "duidi", "duidj",
+                        "duidk", "dujdi", "dukdi", "dujdj", "dukdk", "pi", "ui_source")
+MOMENTUM_FACE_FIELDS = ("flux_u", "flux", "ff", "scoef")
+# Processor.f90:314-340: the face vectors (Si, Sj, Sk, Di, Dj, Dk) per component
+MOMENTUM_FACE_VECTORS = {1: ("Sx", "Sy", "Sz", "Dx", "Dy", "Dz"),
+                         2: ("Sy", "Sx", "Sz", "Dy", "Dx", "Dz"),
+                         3: ("Sz", "Sx", "Sy", "Dz", "Dx", "Dy")}
+# Process/IniPar.f90:22-49
+SCHEME = {"ab": 1, "cn": 2, "fi": 3, "lin": 4, "par": 5, "yes": 10, "no": 11, "cds": 20,
+          "quick": 21, "luds": 22, "minmod": 23, "smart": 24, "avl_smart": 25, "superbee": 26,
+          "gamma": 27}
+
+
+def momentum_assembly(NC, NbC, NS, NONZ, SideC, SidAij, Adia, TypeBC, material, geom, fields,
+                      Nmat, var, blend, blend_tem, urfc, visc, dt, urf, convec=3, cross=3,
+                      diffus=3, inert=4, moin_problem=0):
+    """Process/NewUVW.f90:138-499 with ConvScheme.f90 and CalMinMax.f90
+    restated (momentum_oracle.c), for momentum component ``var``.
+
+    ``geom``: Sx..Dz, f (faces) and volume (cells -NbC..NC); ``fields``: the
+    MOMENTUM_CELL_FIELDS over cells -NbC..NC and MOMENTUM_FACE_FIELDS over
+    faces; material over cells -NbC..NC; blend, blend_tem, urfc per material.
+    Returns (Aval[NONZ], b[NC], Abou[NbC], Asave[NC], rhoUi[NbC+NC+1],
+    status); status 1 = undefined blending, 2 = material out of range.
+    """
+    Aval, b, Asave = np.zeros(NONZ), np.zeros(NC), np.zeros(NC)
+    Abou, rhoUi = np.zeros(max(NbC, 1)), np.zeros(NbC + NC + 1)
+    st = ctypes.c_int()
+    iopt = _i32([Nmat, var, moin_problem, convec, cross, diffus, inert])
+    dopt = _f64([visc, dt, urf])
+    ints = [_i32(SideC), _i32(SidAij), _i32(Adia), _i32(TypeBC), _i32(material), _i32(blend),
+            _i32(blend_tem)]
+    dbl = [_f64(urfc), _f64(geom["f"]), _f64(geom["volume"])]
+    fv = [_f64(geom[k]) for k in MOMENTUM_FACE_VECTORS[var]]
+    ff = [_f64(fields[k]) for k in MOMENTUM_FACE_FIELDS]
+    cf = [_f64(fields[k]) for k in MOMENTUM_CELL_FIELDS]
+    ptrs = [(_D * len(g))(*[_dp(a) for a in g]) for g in (fv, ff, cf)]
+    lib().oracle_newuvw_assembly(int(NC), int(NbC), int(NS), int(NONZ), _ip(iopt), _dp(dopt),
+                                 *[_ip(a) for a in ints], *[_dp(a) for a in dbl], *ptrs,
+                                 _dp(Aval), _dp(b), _dp(Abou), _dp(Asave), _dp(rhoUi),
+                                 ctypes.byref(st))
+    return Aval, b, Abou[:NbC], Asave, rhoUi, st.value

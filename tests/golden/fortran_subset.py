@@ -4,7 +4,10 @@ This is a translator for the small Fortran 90 subset that the Krylov solver
 files of T-FlowS use (Process/CG.f90, BiCG.f90, CGS.f90, Prec1.f90,
 Resid.f90): SUBROUTINE headers, INTEGER/REAL declarations with explicit
 bounds, DO loops with steps, block and one-line IF, GOTO to a label at
-subroutine level, CALL, assignments and the intrinsics sqrt/min/max/real/abs.
+subroutine level, CALL (scalar actual arguments that are variables receive
+the dummy's final value, as pass-by-reference does), assignments including
+whole-array ones (`a = 0.0`, `a = b`) and the intrinsics
+sqrt/min/max/real/abs.
 Each subroutine becomes a Python function.  Real values are numpy float64
 scalars: IEEE binary64 with correctly rounded + - * / and sqrt and IEEE
 results for x/0 (Inf or NaN, no exception), which is what gfortran emits for
@@ -195,7 +198,8 @@ def _logical_lines(text):
 
 
 def translate(text, module_names, params, subroutines):
-    """Translate every SUBROUTINE in `text` to Python source."""
+    """Translate every SUBROUTINE in `text` to Python source; `subroutines`
+    maps each callable subroutine name to its dummy argument names."""
     lines = _logical_lines(text)
     out = []
     i = 0
@@ -283,18 +287,31 @@ def _translate_sub(name, args, body, module_names, params, subroutines):
             if cname not in subroutines:
                 raise SyntaxError(f"call to unknown subroutine {cname}")
             cargs = _split_top(_tokens(m.group(2) or ""))
-            pas = []
-            for ca in cargs:
+            pas, back = [], []
+            dummies = subroutines[cname]
+            for k, ca in enumerate(cargs):
                 if len(ca) == 1 and ca[0][0] == "name" and ca[0][1] in scope.arrays:
                     pas.append(scope.ref(ca[0][1]))
                 else:
                     pas.append(_expr(ca, scope))
-            return f"{cname}(M, {', '.join(pas)})"
+                    if (len(ca) == 1 and ca[0][0] == "name" and ca[0][1] not in scope.params
+                            and k < len(dummies)):
+                        back.append(f"{scope.ref(ca[0][1])} = _r[{dummies[k]!r}]")
+            call = f"{cname}(M, {', '.join(pas)})"
+            return "; ".join([f"_r = {call}"] + back) if back else call
         # assignment: variable or array element, '=', expression
         m = re.match(r"^([a-z_]\w*\s*(?:\([^=]*\))?)\s*=(?!=)(.*)$", st)
         if not m:
             raise SyntaxError(f"unsupported statement {st!r}")
-        lhs = _expr(_tokens(m.group(1)), scope)
+        ltoks = _tokens(m.group(1))
+        if len(ltoks) == 1 and ltoks[0][1] in scope.arrays:
+            # whole-array assignment: from an array of the same shape, or a scalar
+            rtoks = _tokens(m.group(2))
+            lhs = scope.ref(ltoks[0][1])
+            if len(rtoks) == 1 and rtoks[0][0] == "name" and rtoks[0][1] in scope.arrays:
+                return f"_acopy({lhs}, {scope.ref(rtoks[0][1])})"
+            return f"_afill({lhs}, {_expr(rtoks, scope)})"
+        lhs = _expr(ltoks, scope)
         rhs = _expr(_tokens(m.group(2)), scope)
         return f"{lhs} = {rhs}"
 
@@ -389,14 +406,26 @@ def _sqrt(x):
     return np.sqrt(np.float64(x))
 
 
+def _afill(a, v):
+    for k in range(a.off, len(a.buf)):
+        a.buf[k] = v
+
+
+def _acopy(a, b):
+    n = len(a.buf) - a.off
+    a.buf[a.off:] = b.buf[b.off:b.off + n]
+
+
 def load_subroutines(texts, module_names, params):
     """Translate the given Fortran source texts and return {name: function}."""
-    names = set()
+    names = {}
     for t in texts:
-        names.update(m.group(1) for m in re.finditer(r"(?im)^\s*subroutine\s+(\w+)", t))
-    names = {n.lower() for n in names}
+        for line in _logical_lines(t):
+            m = re.match(r"subroutine\s+(\w+)\s*\((.*)\)$", line)
+            if m:
+                names[m.group(1)] = [a.strip() for a in m.group(2).split(",") if a.strip()]
     src = "\n".join(translate(t, module_names, params, names) for t in texts)
     env = {"_Goto": _Goto, "_trip": _trip, "_sqrt": _sqrt, "math": math,
-           "float": np.float64}
+           "float": np.float64, "_afill": _afill, "_acopy": _acopy}
     exec(compile(src, "<fortran_subset>", "exec"), env)
     return {n: env[n] for n in names}, src
