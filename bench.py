@@ -560,6 +560,77 @@ def assembly_block(pkg, dev, n=128, reps=5):
             "cpu_oracle_ms": cpu_s * 1e3, "cpu_cores": 1, "aval_bitwise_vs_oracle": same}
 
 
+def momentum_block(pkg, dev, n=128, reps=5):
+    """The momentum assembly (Process/NewUVW.f90:138-499) of component U on
+    an n^3 perturbed box on the GPU: SMART blending (ConvScheme with the
+    CalMinMax bounds), upwind sums, implicit diffusion, two time levels;
+    inflow on x-min, outflow on x-max, walls elsewhere; seeded fields.  Device
+    time, algorithmic bytes (every input read once, every output written
+    once) against the HBM peak, the one-core CPU restatement beside it."""
+    import numpy as np
+    import torch
+    import oracle
+    msh = pkg.mesh.box_faces(n, n, n, perturb=0.2, seed=7)
+    NC, NbC, NS = msh["NC"], msh["NbC"], msh["NS"]
+    NONZ = int(msh["Acol"][-1])
+    rng = np.random.default_rng(9)
+    m = NbC + NC + 1
+    tb = np.full(m, 2, np.int32)
+    tb[NbC:] = 0
+    tb[NbC - np.arange(1, n * n + 1)] = 1
+    tb[NbC - np.arange(n * n + 1, 2 * n * n + 1)] = 3
+    cpu = {}
+    for k in ("rho_n", "rho_o", "rho_oo"):
+        cpu[k] = rng.uniform(0.5, 1.5, m)
+    for k in oracle.MOMENTUM_CELL_FIELDS[3:]:
+        cpu[k] = rng.uniform(-1.0, 1.0, m)
+    for k in ("flux_u", "flux"):
+        cpu[k] = rng.uniform(-1.0, 1.0, NS)
+    cpu["ff"] = msh["f"].copy()
+    cpu["scoef"] = ((msh["Sx"] * msh["Sx"] + msh["Sy"] * msh["Sy"] + msh["Sz"] * msh["Sz"])
+                    / (msh["Dx"] * msh["Sx"] + msh["Dy"] * msh["Sy"] + msh["Dz"] * msh["Sz"]))
+    material = np.ones(m, np.int32)
+    smart, yes = oracle.SCHEME["smart"], oracle.SCHEME["yes"]
+    opts = dict(visc=1e-2, dt=0.01, urf=0.7)
+    asm = pkg.Assembly.from_faces(msh, tb)
+    fields = {("source" if k == "ui_source" else k): torch.from_numpy(cpu[k]).to(dev)
+              for k in oracle.MOMENTUM_CELL_FIELDS + oracle.MOMENTUM_FACE_FIELDS}
+    fields.update(material=torch.from_numpy(material).to(dev),
+                  blend=torch.tensor([smart], dtype=torch.int32, device=dev),
+                  blend_tem=torch.tensor([yes], dtype=torch.int32, device=dev),
+                  urfc=torch.tensor([0.9], dtype=torch.float64, device=dev))
+    aval = torch.empty(NONZ, dtype=torch.float64, device=dev)
+    b = torch.empty(NC, dtype=torch.float64, device=dev)
+    abou = torch.zeros(NbC, dtype=torch.float64, device=dev)
+    asave = torch.empty(NC, dtype=torch.float64, device=dev)
+    rhoui = torch.empty(m, dtype=torch.float64, device=dev)
+    secs = []
+    for _ in range(reps + 2):
+        secs.append(asm.newuvw(1, fields, aval, b, abou, asave, rhoui, **opts)["seconds"])
+    sec = min(secs[2:])
+    # inputs once: 12 doubles + c1, c2, SidAij per face; 15 cell fields,
+    # material, TypeBC, volume per cell; Adia; outputs Aval, b, Asave, rhoUi, Abou
+    byts = (NS * (12 * 8 + 4 * 4) + m * (15 * 8 + 4 + 4 + 8) + NC * 4
+            + 8 * (NONZ + 2 * NC + m + NbC))
+    gpu_aval, gpu_b = aval.cpu().numpy(), b.cpu().numpy()
+    asm.close()
+    geom = {k: msh[k] for k in ("Sx", "Sy", "Sz", "Dx", "Dy", "Dz", "f")}
+    geom["volume"] = msh["volume"]
+    t0 = time.perf_counter()
+    ref = oracle.momentum_assembly(NC, NbC, NS, NONZ, msh["SideC"], msh["SidAij"], msh["Adia"],
+                                   tb, material, geom, cpu, 1, 1, np.array([smart], np.int32),
+                                   np.array([yes], np.int32), np.array([0.9]), **opts)
+    cpu_s = time.perf_counter() - t0
+    same = bool(np.array_equal(gpu_aval.view(np.uint64), ref[0].view(np.uint64))
+                and np.array_equal(gpu_b.view(np.uint64), ref[1].view(np.uint64)))
+    peak, _ = load_peaks()
+    return {"workload": f"NewUVW momentum assembly (U), {n}^3 perturbed box ({NC} cells, "
+                        f"{NS} faces), SMART blending, inflow/outflow/walls",
+            "ms": sec * 1e3, "gbs": byts / sec / 1e9, "frac": byts / sec / 1e9 / peak,
+            "algorithmic_bytes": byts, "cpu_oracle_ms": cpu_s * 1e3, "cpu_cores": 1,
+            "aval_b_bitwise_vs_oracle": same}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -588,11 +659,22 @@ def main():
                     help="fixed launch shape (256 threads, one slice per warp)")
     ap.add_argument("--ic-compare-scale", type=int, default=256,
                     help="edge of the IC mixed-vs-FP64 comparison (0 = skip)")
+    ap.add_argument("--block", default=None, choices=["calcps", "newuvw"],
+                    help="run only this assembly block on a --scale^3 box (default 128), "
+                         "print its JSON and exit (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.block:
+        import torch
+        import __graft_entry__ as ge
+        pkg = ge.load_package()
+        pkg.load_library()
+        fn = {"calcps": assembly_block, "newuvw": momentum_block}[args.block]
+        print(json.dumps(fn(pkg, torch.device("cuda", 0), n=args.scale or 128)), flush=True)
+        return
 
     import numpy as np
     import torch
@@ -712,6 +794,7 @@ def main():
         line["simple_step"] = simple_step(pkg, dev, autotune=not args.no_autotune)
         torch.cuda.empty_cache()
         line["assembly_calcps"] = assembly_block(pkg, dev)
+        line["assembly_newuvw"] = momentum_block(pkg, dev)
         torch.cuda.empty_cache()
 
     if rank == 0 and (args.compare_scale or args.ic_compare_scale):

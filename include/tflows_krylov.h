@@ -296,8 +296,8 @@ void tflows_mesh_free(tflows_mesh *m);
 int tflows_topolm(int NC, int NS, const int *SideC, int *Acol, int *Arow,
                   int *Adia, int *SidAij, int *NONZ);
 
-/* ---- pressure-correction assembly on the GPU ------------------------------ */
-/* Mesh data of the assembly, resident on the device (host arrays in, copied):
+/* ---- pressure-correction and momentum assembly on the GPU ---------------- */
+/* Mesh data of the assemblies, resident on the device (host arrays in, copied):
  * SideC(0:2,NS) and SidAij(2,NS) as the reference holds them (column-major),
  * Adia(NC) 1-based, TypeBC(-NbC:NC) and volume(-NbC:NC) passed at their
  * element -NbC, face geometry Sx..Sz, Dx..Dz, f(1:NS) (Library/GeoLoa.f90).
@@ -337,6 +337,59 @@ int tflows_calcps_assemble_device(tflows_assembly *a, int Nmat, double dt,
                                   double *aval, double *b, double *abou,
                                   double *flux, double *errmax, void *stream,
                                   double *seconds);
+
+/* Inputs of the momentum assembly of one component Ui (NewUVW's dummies and
+ * the module fields it reads), all device arrays.  Cell arrays span cells
+ * -NbC..NC (element c at [c + NbC]); face arrays faces 1..NS; material
+ * arrays materials 1..Nmat (element m at [m - 1]).  dUidi..dUkdk are the
+ * seven gradient dummies of NewUVW in its order (for U: Ux, Uy, Uz, Vx, Wx,
+ * Vy, Wz; Processor.f90:314-340 gives V and W). */
+typedef struct tflows_newuvw_fields {
+    const int *material;                   /* material(c), 1..Nmat */
+    const double *rho_n, *rho_o, *rho_oo;  /* Rho % n, o, oo */
+    const double *ui_n, *ui_o, *ui_oo;     /* Ui % n, o, oo (after the old-value shift) */
+    const double *duidi, *duidj, *duidk, *dujdi, *dukdi, *dujdj, *dukdk;
+    const double *pi;                      /* Pi: the pressure-gradient component */
+    const double *source;                  /* Ui % source */
+    const double *flux_u;                  /* faces: Flux_u, the convected mass flux */
+    const double *flux;                    /* faces: Flux, orients the blended schemes */
+    const double *ff;                      /* faces: fF */
+    const double *scoef;                   /* faces: Scoef; NULL = |S|^2/(S.d) of the
+                                              mesh, as Process/Calc3.f90:22-47 forms it */
+    const int *blend, *blend_tem;          /* materials: BLEND, BLEND_TEM codes */
+    const double *urfc;                    /* materials: URFC */
+} tflows_newuvw_fields;
+
+/* Scalars of the same call.  Codes as Process/IniPar.f90:22-49 sets them:
+ * AB 1, CN 2, FI 3, LIN 4, PAR 5, YES 10, NO 11, CDS 20, QUICK 21, LUDS 22,
+ * MINMOD 23, SMART 24, AVL_SMART 25, SUPERBEE 26, GAMMA 27. */
+typedef struct tflows_newuvw_params {
+    int var;           /* 1, 2, 3: the component; picks the face vectors
+                          (Si..Dk, Processor.f90:314-340) and Asave on 1 */
+    int nmat;          /* Nmat */
+    int moin_problem;  /* Moin_Problem(): 4 gives VISeff = VISc * RhoS */
+    int convec, cross, diffus, inert;  /* CONVEC, CROSS, DIFFUS, INERT */
+    double visc, dt, urf;              /* VISc, dt, U % URF */
+} tflows_newuvw_params;
+
+/* Replaces the assembly part of SUBROUTINE NewUVW (Process/NewUVW.f90:
+ * 138-499, with ConvScheme.f90 and CalMinMax.f90) for one component:
+ * Aval(1:NONZ) <- the momentum matrix, b(1:NC) <- its right-hand side,
+ * Abou(-NbC:-1) <- 0 and -A12-D12 on BUFFER faces, asave(1:NC) <- the
+ * diagonal before under-relaxation when var == 1 (may be NULL),
+ * rhoui(-NbC:NC) <- Rho % n * Ui % n, the unknown the solve updates in place
+ * (may be NULL).  Ui % o / oo must already hold the shifted old values and
+ * Ui % source the source term (NewUVW.f90:153-199 stay with the caller).
+ * Aval, b, Abou and Asave are bit-identical to the reference's sequential
+ * loops.  A face between a material blending with YES and one with NO hands
+ * ConvScheme a code it does not handle (the reference then reads an unset
+ * local): TFLOWS_BAD_INPUT, as for material indices outside 1..nmat.  The
+ * call waits for the stream to read that check; *seconds (may be NULL) <-
+ * device time. */
+int tflows_newuvw_assemble_device(tflows_assembly *a, const tflows_newuvw_params *params,
+                                  const tflows_newuvw_fields *fields, double *aval,
+                                  double *b, double *abou, double *asave, double *rhoui,
+                                  void *stream, double *seconds);
 
 /* ---- allocation-free solve ------------------------------------------------ */
 /* No counterpart in the reference.  For callers that may not allocate GPU

@@ -19,8 +19,9 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libtflows_krylov.so")
 SOURCES = ("krylov.cu", "krylov_fma.cu", "shim.cu", "noalloc.cu", "tune.cu", "assembly.cu",
-           "meshio.cpp")
-HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "solver_entry.cuh", "internal.h")
+           "momentum.cu", "meshio.cpp")
+HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "solver_entry.cuh", "internal.h",
+           "assembly_internal.h")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -147,6 +148,21 @@ class CalcpsFields(ctypes.Structure):
                                                  "px", "py", "pz", "asave")]
 
 
+NEWUVW_FIELDS = ("material", "rho_n", "rho_o", "rho_oo", "ui_n", "ui_o", "ui_oo", "duidi",
+                 "duidj", "duidk", "dujdi", "dukdi", "dujdj", "dukdk", "pi", "source", "flux_u",
+                 "flux", "ff", "scoef", "blend", "blend_tem", "urfc")
+
+
+class NewuvwFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in NEWUVW_FIELDS]
+
+
+class NewuvwParams(ctypes.Structure):
+    _fields_ = ([(n, ctypes.c_int) for n in ("var", "nmat", "moin_problem", "convec", "cross",
+                                             "diffus", "inert")]
+                + [(n, ctypes.c_double) for n in ("visc", "dt", "urf")])
+
+
 _SOLVER = [_I, _I, _I, _D, _I, _I, _I, _D, _D, _D, _I, _I, _D, _D, _D]
 
 SIGNATURES = {
@@ -192,6 +208,9 @@ SIGNATURES = {
                                        ctypes.POINTER(CalcpsFields), _VP, _VP, _VP, _VP,
                                        ctypes.POINTER(ctypes.c_double), _VP,
                                        ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "tflows_newuvw_assemble_device": ([_VP, ctypes.POINTER(NewuvwParams),
+                                       ctypes.POINTER(NewuvwFields), _VP, _VP, _VP, _VP, _VP,
+                                       _VP, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "tflows_mesh_read": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(Mesh))],
                          ctypes.c_int),
     "tflows_mesh_free": ([ctypes.POINTER(Mesh)], None),

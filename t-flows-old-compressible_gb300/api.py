@@ -388,8 +388,10 @@ class Plan:
 
 
 class Assembly:
-    """The pressure-correction assembly of Process/CalcPS.f90:49-202 on the
-    GPU (tflows_assembly_create / tflows_calcps_assemble_device).
+    """The pressure-correction assembly of Process/CalcPS.f90:49-202 and the
+    momentum assembly of Process/NewUVW.f90:138-499 on the GPU
+    (tflows_assembly_create / tflows_calcps_assemble_device /
+    tflows_newuvw_assemble_device).
 
     Mesh arrays as the reference holds them: SideC (NS, 3) = SideC(0:2, NS),
     SidAij (NS, 2), Adia 1-based, TypeBC and volume over cells -NbC..NC,
@@ -432,6 +434,50 @@ class Assembly:
         if st != OK:
             raise SolverError(st, last_error())
         return {"errmax": em.value if errmax else None, "seconds": sec.value}
+
+    # Process/IniPar.f90:22-49
+    CODES = {"ab": 1, "cn": 2, "fi": 3, "lin": 4, "par": 5, "yes": 10, "no": 11, "cds": 20,
+             "quick": 21, "luds": 22, "minmod": 23, "smart": 24, "avl_smart": 25,
+             "superbee": 26, "gamma": 27}
+
+    def newuvw(self, var, fields, aval, b, abou, asave=None, rhoui=None, *, nmat=1, visc,
+               dt, urf, convec=3, cross=3, diffus=3, inert=4, moin_problem=0):
+        """Momentum assembly of component ``var`` (1, 2, 3) into aval (NONZ),
+        b (NC), abou (NbC, cells -NbC..-1), asave (NC, var 1 only; optional)
+        and rhoui (cells -NbC..NC; optional) on torch's current stream.
+        ``fields``: CUDA tensors keyed as tflows_newuvw_fields -- int32
+        material (cells), blend and blend_tem (materials); float64 cell fields
+        over -NbC..NC, face fields over 1..NS, urfc over materials; ``scoef``
+        may be absent (|S|^2/(S.d) of the mesh); rho_oo and ui_oo only for
+        inert == PAR (5).  Returns {seconds}."""
+        ptrs = {}
+        for k in _native.NEWUVW_FIELDS:
+            t = fields.get(k)
+            if t is None:
+                ptrs[k] = None
+                continue
+            want = 4 if k in ("material", "blend", "blend_tem") else 8
+            if not (t.is_cuda and t.dtype.itemsize == want and t.is_contiguous()):
+                raise TypeError(f"field {k!r} must be a contiguous CUDA "
+                                f"{'int32' if want == 4 else 'float64'} tensor")
+            ptrs[k] = t.data_ptr()
+        outs = [aval, b, abou] + [t for t in (asave, rhoui) if t is not None]
+        for t in outs:
+            if not (t.is_cuda and t.dtype.itemsize == 8 and t.is_contiguous()):
+                raise TypeError("outputs must be contiguous CUDA float64 tensors")
+        F = _native.NewuvwFields(**ptrs)
+        P = _native.NewuvwParams(var=int(var), nmat=int(nmat), moin_problem=int(moin_problem),
+                                 convec=int(convec), cross=int(cross), diffus=int(diffus),
+                                 inert=int(inert), visc=float(visc), dt=float(dt),
+                                 urf=float(urf))
+        sec = ctypes.c_double()
+        st = lib().tflows_newuvw_assemble_device(
+            self._h, ctypes.byref(P), ctypes.byref(F), _ptr(aval), _ptr(b), _ptr(abou),
+            _ptr(asave) if asave is not None else None,
+            _ptr(rhoui) if rhoui is not None else None, _stream(), ctypes.byref(sec))
+        if st != OK:
+            raise SolverError(st, last_error())
+        return {"seconds": sec.value}
 
     def close(self):
         if self._h:

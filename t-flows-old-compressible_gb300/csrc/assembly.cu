@@ -15,6 +15,7 @@
 // sum_c volume(c) is a deterministic tree reduction, not the reference's
 // left-to-right sum, so b differs from the reference by the rounding of that
 // one scalar.
+#include "assembly_internal.h"
 #include "internal.h"
 #include "tflows_krylov.h"
 
@@ -25,13 +26,8 @@
 
 namespace {
 
-// Library/allp_mod.f90:16-24
-enum : int { kInflow = 1, kOutflow = 3, kConvect = 5, kBuffer = 11, kPressure = 12 };
-
 // What a face adds to its cells (set by the face pass, read by the cell pass).
 enum : unsigned char { kDiag1 = 1, kB1 = 2, kCell2 = 4 };
-
-constexpr int kAsmBlock = 256;
 
 struct FaceGeom {
     const double* sx;
@@ -270,23 +266,6 @@ int asm_fail(int status, const std::string& msg) { return tflows::report_status(
 
 }  // namespace
 
-struct tflows_assembly {
-    int device = 0;
-    int NC = 0, NbC = 0, NS = 0, NONZ = 0;
-    int nblocks = 0;
-    int *c1 = nullptr, *c2 = nullptr, *sid1 = nullptr, *sid2 = nullptr;
-    int *adia = nullptr, *type = nullptr, *cf_ptr = nullptr, *pos1 = nullptr, *pos2 = nullptr;
-    double* geom = nullptr;  // Sx Sy Sz Dx Dy Dz f SMDPN (1-f), NS each
-    double* vol = nullptr;   // -NbC..NC
-    double* vdiva = nullptr; // volume / Asave of the current call, -NbC..NC
-    double* slot_a = nullptr;  // per (cell, face): A12 and the flux the face adds
-    double* slot_f = nullptr;
-    unsigned char* slot_k = nullptr;
-    double* parts = nullptr;  // 2 * nblocks partial sums, then the two totals
-    unsigned long long* errmax = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-};
-
 extern "C" {
 
 void tflows_assembly_destroy(tflows_assembly* a) {
@@ -295,7 +274,9 @@ void tflows_assembly_destroy(tflows_assembly* a) {
     for (void* p : {(void*)a->c1, (void*)a->c2, (void*)a->sid1, (void*)a->sid2, (void*)a->adia,
                     (void*)a->type, (void*)a->cf_ptr, (void*)a->pos1, (void*)a->pos2,
                     (void*)a->geom, (void*)a->vol, (void*)a->slot_a, (void*)a->slot_f,
-                    (void*)a->slot_k, (void*)a->parts, (void*)a->errmax, (void*)a->vdiva})
+                    (void*)a->slot_k, (void*)a->parts, (void*)a->errmax, (void*)a->vdiva,
+                    (void*)a->slot_face, (void*)a->bnd_ptr, (void*)a->bnd_face,
+                    a->mom_rec, (void*)a->mom_cells, (void*)a->mom_err})
         if (p) cudaFree(p);
     if (a->ev0) cudaEventDestroy(a->ev0);
     if (a->ev1) cudaEventDestroy(a->ev1);
@@ -340,9 +321,25 @@ int tflows_assembly_create(tflows_assembly** out, int NC, int NbC, int NS, int N
     for (int c = 1; c <= NC; ++c) ptr[c] = ptr[c - 1] + deg[c];
     std::vector<int> pos1(std::max(NS, 1)), pos2(std::max(NS, 1), -1);
     std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    std::vector<int> slot_face(std::max(ptr[NC], 1));
     for (int s = 0; s < NS; ++s) {
         pos1[s] = fill[c1[s] - 1]++;
-        if (c2[s] > 0) pos2[s] = fill[c2[s] - 1]++;
+        slot_face[pos1[s]] = s;
+        if (c2[s] > 0) {
+            pos2[s] = fill[c2[s] - 1]++;
+            slot_face[pos2[s]] = ~s;
+        }
+    }
+    // each boundary cell's faces in increasing order
+    std::vector<int> bptr(NbC + 1, 0);
+    for (int s = 0; s < NS; ++s)
+        if (c2[s] < 0) ++bptr[c2[s] + NbC + 1];
+    for (int j = 0; j < NbC; ++j) bptr[j + 1] += bptr[j];
+    std::vector<int> bface(std::max(bptr[NbC], 1));
+    {
+        std::vector<int> bf(bptr.begin(), bptr.end() - 1);
+        for (int s = 0; s < NS; ++s)
+            if (c2[s] < 0) bface[bf[c2[s] + NbC]++] = s;
     }
     const size_t nslot = std::max(ptr[NC], 1);
     if (device >= 0 && cudaSetDevice(device) != cudaSuccess)
@@ -368,6 +365,9 @@ int tflows_assembly_create(tflows_assembly** out, int NC, int NbC, int NS, int N
     if (e == cudaSuccess) e = upload(&a->cf_ptr, ptr.data(), ptr.size());
     if (e == cudaSuccess) e = upload(&a->pos1, pos1.data(), pos1.size());
     if (e == cudaSuccess) e = upload(&a->pos2, pos2.data(), pos2.size());
+    if (e == cudaSuccess) e = upload(&a->slot_face, slot_face.data(), slot_face.size());
+    if (e == cudaSuccess) e = upload(&a->bnd_ptr, bptr.data(), bptr.size());
+    if (e == cudaSuccess) e = upload(&a->bnd_face, bface.data(), bface.size());
     if (e == cudaSuccess) e = upload(&a->geom, geom.data(), geom.size());
     if (e == cudaSuccess) e = upload(&a->vol, volume, (size_t)NbC + NC + 1);
     if (e == cudaSuccess && NS > 0) {
