@@ -88,12 +88,9 @@ __global__ void __launch_bounds__(kAsmBlock) vdiva_kernel(int n, const double* _
 // One thread per face: CalcPS.f90:71-164 for face s = i + 1.
 __global__ void __launch_bounds__(kAsmBlock) face_kernel(int NS, int NbC, const int* __restrict__ c1s,
                                                          const int* __restrict__ c2s,
-                                                         const int* __restrict__ sid1,
-                                                         const int* __restrict__ sid2,
                                                          const int* __restrict__ pos1,
                                                          const int* __restrict__ pos2, FaceGeom g,
-                                                         CellFields F, double* __restrict__ aval,
-                                                         double* __restrict__ abou,
+                                                         CellFields F, double* __restrict__ abou,
                                                          double* __restrict__ flux,
                                                          double* __restrict__ slot_a,
                                                          double* __restrict__ slot_f,
@@ -112,9 +109,7 @@ __global__ void __launch_bounds__(kAsmBlock) face_kernel(int NS, int NbC, const 
             const double Wrs = f * F.rho_n[c1] * F.w[c1] + omf * F.rho_n[k2] * F.w[k2];
             A12 = 0.5 * S * (F.vdiva[c1] + F.vdiva[k2]);
             if (c2 > 0) {
-                aval[sid1[i]] = -A12;
-                aval[sid2[i]] = -A12;
-                kd = kDiag1 | kB1 | kCell2;
+                kd = kDiag1 | kB1 | kCell2;  // the cell pass sets Aval(SidAij(:, s)) = -A12
             } else {
                 abou[k2] = -A12;
                 kd = kDiag1 | kB1;
@@ -163,9 +158,13 @@ __global__ void __launch_bounds__(kAsmBlock) face_kernel(int NS, int NbC, const 
 // (186-193) and this cell's terms of the two sums of the mean.  The face
 // pass left each contribution in the cell's own list (entries cf_ptr[i] ..
 // cf_ptr[i+1]-1, faces in increasing order), so the reads are contiguous.
+// The cell also sets its row's off-diagonal entries Aval(SidAij) = -A12 in
+// face order, so where two faces join the same cells (one entry) the later
+// face's value stays, as in the reference.
 __global__ void __launch_bounds__(kAsmBlock) cell_kernel(
     int NC, int NbC, int Nmat, double dt, const int* __restrict__ cf_ptr,
-    const int* __restrict__ adia, const double* __restrict__ slot_a,
+    const int* __restrict__ slot_face, const int* __restrict__ sid1,
+    const int* __restrict__ sid2, const int* __restrict__ adia, const double* __restrict__ slot_a,
     const double* __restrict__ slot_f, const unsigned char* __restrict__ slot_k, CellFields F,
     double* __restrict__ aval, double* __restrict__ b, double* __restrict__ part_sum,
     double* __restrict__ part_vol, unsigned long long* __restrict__ errmax_bits) {
@@ -194,6 +193,11 @@ __global__ void __launch_bounds__(kAsmBlock) cell_kernel(
                     }
                 }
             if (diag) aval[adia[i]] = d;
+            for (int e = e0; e < e1; ++e) {
+                const int sf = slot_face[e];
+                const int o = sf >= 0 ? sid1[sf] : sid2[~sf];
+                if (o >= 0) aval[o] = -slot_a[e];
+            }
             my_max = max(my_max, (unsigned long long)__double_as_longlong(fabs(bb)));
             const int c = i + 1 + NbC;
             for (int m = 0; m < Nmat; ++m) {
@@ -425,16 +429,16 @@ int tflows_calcps_assemble_device(tflows_assembly* a, int Nmat, double dt,
     }
     const int fb = std::max(1, std::min((a->NS + kAsmBlock - 1) / kAsmBlock, 65535));
     if (e == cudaSuccess && a->NS > 0) {
-        face_kernel<<<fb, kAsmBlock, 0, s>>>(a->NS, a->NbC, a->c1, a->c2, a->sid1, a->sid2,
-                                             a->pos1, a->pos2, g, F, aval, abou, flux,
-                                             a->slot_a, a->slot_f, a->slot_k);
+        face_kernel<<<fb, kAsmBlock, 0, s>>>(a->NS, a->NbC, a->c1, a->c2, a->pos1, a->pos2, g,
+                                             F, abou, flux, a->slot_a, a->slot_f, a->slot_k);
         e = cudaGetLastError();
     }
     double* ps = a->parts;
     double* pv = a->parts + a->nblocks;
     double* tot = a->parts + 2 * a->nblocks;
     if (e == cudaSuccess) {
-        cell_kernel<<<a->nblocks, kAsmBlock, 0, s>>>(a->NC, a->NbC, Nmat, dt, a->cf_ptr, a->adia,
+        cell_kernel<<<a->nblocks, kAsmBlock, 0, s>>>(a->NC, a->NbC, Nmat, dt, a->cf_ptr,
+                                                     a->slot_face, a->sid1, a->sid2, a->adia,
                                                      a->slot_a, a->slot_f, a->slot_k, F, aval, b,
                                                      ps, pv, a->errmax);
         e = cudaGetLastError();

@@ -203,3 +203,28 @@ def test_mesh_files_to_gpu_solve(tmp_path):
     assert np.linalg.norm(b.cpu().numpy() - M @ x.cpu().numpy()) < 2 * tol
     asm.close()
     topo.close()
+
+
+def test_assembly_two_faces_between_the_same_cells():
+    """Two faces joining the same pair of cells share one off-diagonal entry
+    (TopolM maps both to it): the reference assigns -A12 face by face, so the
+    later face's value stays; both faces add to the diagonals.  The GPU
+    matches the oracle bit for bit."""
+    d = _box_case((6, 5, 4), 2, 1)
+    inner = np.nonzero(d["SideC"][:, 2] > 0)[0]
+    dup = int(inner[len(inner) // 3])
+    order = np.r_[np.arange(dup + 1), dup, np.arange(dup + 1, d["NS"])]
+    for k in ("SideC", "Sx", "Sy", "Sz", "Dx", "Dy", "Dz", "f"):
+        d[k] = np.ascontiguousarray(d[k][order])
+    d["Sx"][dup + 1] *= 1.5  # the second face differs, so the order shows
+    d["NS"] += 1
+    Acol, Arow, Adia, sid = oracle.topolm(d["NC"], d["SideC"][:, 1:])
+    d.update(Acol=Acol, Arow=Arow, Adia=Adia, SidAij=sid, NONZ=int(Acol[-1]))
+    dt = 0.02
+    ref = oracle.calcps_assembly(d["NC"], d["NbC"], d["NS"], d["NONZ"], 1, dt, d["SideC"],
+                                 d["SidAij"], d["Adia"], d["TypeBC"],
+                                 {k: d[k] for k in oracle.FACE_GEOM},
+                                 {k: d[k] for k in oracle.CELL_FIELDS})
+    got = _run_gpu(d, 1, dt, abou_in=np.zeros(max(d["NbC"], 1)))
+    ra = ref[2].copy()
+    _check(got, (ref[0], ref[1], ra, ref[3], ref[4]))
