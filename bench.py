@@ -383,6 +383,49 @@ def cfg2_methods(pkg, dev, topo, s, val, b, reps=3):
     return out
 
 
+def cfg1_latency(pkg, dev, reps=20):
+    """Config 1: the 32^3 Jacobi-CG system (32,768 rows), FP64 in reference
+    arithmetic and with fused multiply-adds, device-resident and through the
+    Fortran-facing C ABI, against the one-core oracle.  Its 2.8 MB of values
+    fit in L2, so a solve is bound by the latency of its grid barriers, not by
+    HBM: reported per solve and per iteration, not against the roofline."""
+    import numpy as np
+    import torch
+    import oracle
+    s = make_workload(pkg, "cfg1", None)
+    topo = pkg.Topology.from_system(s)
+    val = torch.from_numpy(s.A[:-1].copy()).to(dev)
+    b = torch.from_numpy(s.b.copy()).to(dev)
+    x = torch.zeros(s.N, dtype=torch.float64, device=dev)
+    out = {"workload": f"{s.name}: CG + diagonal to 1e-8*||b|| (absolute), x0=0", "n": s.N}
+    for label, precision in (("fp64", pkg.FP64), ("fp64_fma", pkg.FP64_FMA)):
+        opts = pkg.options(precision=precision, autotune=1)
+        el, res = device_solves(pkg, topo, val, b, x, "cg", 1, s.tol, opts, reps, 3)
+        r = res[-1]
+        out[label] = {"us_per_solve": 1e6 * el / reps, "iterations": r["iterations"],
+                      "us_per_iteration": 1e6 * el / reps / max(r["iterations"], 1),
+                      "status": r["status"], "block_size": r["block_size"],
+                      "grid_blocks": r["grid_blocks"]}
+    pkg.set_options(precision=pkg.FP64)
+    xh, rh = s.x.copy(), s.b.copy()
+    pkg.cg(s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab, xh, rh, 1, 20000, s.tol)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        xh, rh = s.x.copy(), s.b.copy()
+        pkg.cg(s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab, xh, rh, 1, 20000, s.tol)
+    out["c_abi_us_per_solve"] = 1e6 * (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    xo, _, ito, _, _ = oracle.solve("cg", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
+                                    s.x, s.b, 1, 20000, s.tol)
+    out["cpu_oracle_us_per_solve"] = 1e6 * (time.perf_counter() - t0)
+    out["cpu_cores"] = 1
+    out["oracle_iterations"] = ito
+    out["rel_err_vs_oracle"] = float(np.abs(xh - xo).max() / np.abs(xo).max())
+    pkg.set_options()
+    topo.close()
+    return out
+
+
 def adjoint_cfg5(pkg, dev, reps=3):
     """Config 5: 64^3 variable-density pressure assembled differentiably from
     its float32 face coefficients, loss 0.5||x - x_t||^2, one forward solve
@@ -659,9 +702,9 @@ def main():
                     help="fixed launch shape (256 threads, one slice per warp)")
     ap.add_argument("--ic-compare-scale", type=int, default=256,
                     help="edge of the IC mixed-vs-FP64 comparison (0 = skip)")
-    ap.add_argument("--block", default=None, choices=["calcps", "newuvw"],
-                    help="run only this assembly block on a --scale^3 box (default 128), "
-                         "print its JSON and exit (for profiling)")
+    ap.add_argument("--block", default=None, choices=["calcps", "newuvw", "cfg1"],
+                    help="run only this block (an assembly on a --scale^3 box, default 128, "
+                         "or the config-1 latency block), print its JSON and exit")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -672,8 +715,12 @@ def main():
         import __graft_entry__ as ge
         pkg = ge.load_package()
         pkg.load_library()
+        dev = torch.device("cuda", 0)
+        if args.block == "cfg1":
+            print(json.dumps(cfg1_latency(pkg, dev)), flush=True)
+            return
         fn = {"calcps": assembly_block, "newuvw": momentum_block}[args.block]
-        print(json.dumps(fn(pkg, torch.device("cuda", 0), n=args.scale or 128)), flush=True)
+        print(json.dumps(fn(pkg, dev, n=args.scale or 128)), flush=True)
         return
 
     import numpy as np
@@ -789,6 +836,7 @@ def main():
     del val, b, x, y, xs
     torch.cuda.empty_cache()
     if rank == 0 and not args.no_extras:
+        line["cfg1_latency"] = cfg1_latency(pkg, dev)
         line["adjoint_cfg5"] = adjoint_cfg5(pkg, dev)
         torch.cuda.empty_cache()
         line["simple_step"] = simple_step(pkg, dev, autotune=not args.no_autotune)

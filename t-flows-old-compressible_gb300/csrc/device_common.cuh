@@ -199,13 +199,17 @@ __device__ __forceinline__ void grid_init(Grid& g, DevCtl* ctl, double* partials
 
 // Grid-wide barrier with release/acquire ordering (every write before the
 // barrier is visible to every read after it).  Returns false when the
-// launch was aborted (timeout or error raised anywhere).
+// launch was aborted (timeout or error raised anywhere).  The block's
+// threads meet at __syncthreads, then thread 0 arrives with a release add
+// and waits with acquire loads; the release is cumulative over the writes
+// the block barrier ordered before it and the acquire orders every read
+// after the closing block barrier, so no separate fence is needed (a fence
+// on each side cost 0.9 us of a 6.6 us barrier with 304 blocks).
 __device__ __forceinline__ bool grid_sync(Grid& g, int where) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         g.target += (unsigned long long)g.nblocks;
-        __threadfence();
         if (g.stall && g.bid == 0) g.stall = 0;  // withheld: the barrier cannot complete
         else red_release_add_u64(&g.ctl->bar, 1ull);
         int ok = 1;
@@ -223,7 +227,6 @@ __device__ __forceinline__ bool grid_sync(Grid& g, int where) {
                 }
             }
         }
-        __threadfence();
         if (ld_relaxed_s32(&g.ctl->abort)) ok = 0;
         s_ok = ok;
     }
@@ -231,15 +234,25 @@ __device__ __forceinline__ bool grid_sync(Grid& g, int where) {
     return s_ok != 0;
 }
 
-// Publish this block's K partial sums into slot range [slot, slot+K).
+// Publish this block's K partial sums into slot range [slot, slot+K): the
+// sums of block_sums, stored by thread 0, which forms them (the grid_sync
+// that follows every publish orders the stores before its arrival).
 template <int K>
 __device__ __forceinline__ void publish(Grid& g, int slot, const double (&v)[K]) {
     __shared__ double sm[K * 32];
-    __shared__ double out[K];
-    block_sums<K>(v, sm, out);
-    if (threadIdx.x == 0) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-        for (int k = 0; k < K; ++k) g.partials[(size_t)(slot + k) * g.nblocks + g.bid] = out[k];
+    for (int k = 0; k < K; ++k) {
+        const double s = warp_sum(v[k]);
+        if (lane == 0) sm[k * nw + warp] = s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const double s = warp_sum(lane < nw ? sm[k * nw + lane] : 0.0);
+            if (lane == 0) g.partials[(size_t)(slot + k) * g.nblocks + g.bid] = s;
+        }
     }
 }
 
@@ -253,8 +266,18 @@ __device__ __forceinline__ void totals(Grid& g, int slot, double (&res)[K]) {
         for (int k = 0; k < K; ++k) {
             const long long* src =
                 reinterpret_cast<const long long*>(g.partials + (size_t)(slot + k) * g.nblocks);
+            // each lane's partials in increasing block order, loads issued
+            // eight at a time ahead of their sums
             double s = 0.0;
-            for (int b = g.lane; b < g.nblocks; b += 32) s += __longlong_as_double(ld_relaxed_s64(src + b));
+            for (int b0 = g.lane; b0 < g.nblocks; b0 += 32 * 8) {
+                long long w[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    w[u] = b0 + 32 * u < g.nblocks ? ld_relaxed_s64(src + b0 + 32 * u) : 0;
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (b0 + 32 * u < g.nblocks) s += __longlong_as_double(w[u]);
+            }
             s = warp_sum(s);
             if (g.lane == 0) s_tot[k] = s;
         }
@@ -262,7 +285,9 @@ __device__ __forceinline__ void totals(Grid& g, int slot, double (&res)[K]) {
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < K; ++k) res[k] = s_tot[k];
-    __syncthreads();
+    // no closing block barrier: the next write of s_tot comes after the
+    // next grid_sync, whose opening __syncthreads every thread reaches after
+    // reading these totals
 }
 
 }  // namespace tflows
