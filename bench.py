@@ -59,6 +59,16 @@ def profiled_traffic(kernel, workload, method, prec):
         return None
 
 
+def profiled_limiter(kernel, workload, method, prec):
+    """What the committed ncu summary shows bounding this kernel on this
+    workload (profiles/traffic.json, "limiters"), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get("limiters", {}).get(f"{kernel}|{workload}|{method}|{prec}")
+    except Exception:
+        return None
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
         os.environ.get("LOCAL_RANK", "0"))
@@ -791,6 +801,7 @@ def main():
                                    "fp64_fma": "fma::krylov_kernel<double>",
                                    "mixed": "fma::mixed_kernel"}[args.precision]
                                   + " (one persistent launch per solve)",
+                        "limiter": profiled_limiter(kname, s.name, method, prec),
                         "peak_kind": peak_kind}
 
     if not args.no_e2e:
