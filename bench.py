@@ -835,7 +835,8 @@ def main():
     sl = (s.N + 31) // 32
     for tag, fp32, sv in (("spmv_fp64", False, 8), ("spmv_fp32", True, 4)):
         sec = topo.spmv(val, xs, y, repeat=20, fp32=fp32)
-        byts = s.nnz * (sv + 4.0) + 8.0 * (sl + 1) + 2.0 * s.N * sv
+        idx = s.N if topo.patterns else 4.0 * s.nnz  # pattern id per row, or a column per entry
+        byts = s.nnz * sv + idx + 8.0 * (sl + 1) + 2.0 * s.N * sv
         line[tag] = {"gbs": byts / sec / 1e9, "frac": byts / sec / 1e9 / peak, "us": sec * 1e6,
                      "bytes": byts}
     line["clocks"] = clk

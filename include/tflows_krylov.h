@@ -192,6 +192,13 @@ void tflows_topology_destroy(tflows_topology *topo);
  * for the entry k at (i,j); -1 where the pattern has no such entry.
  * Device int array of nnz elements, valid while the topology lives. */
 const int *tflows_topology_transpose_map(tflows_topology *topo);
+/* Column patterns of the topology's products: the number of distinct
+ * per-row offset tuples (column - row) the products read instead of column
+ * indices (1..255), or 0 when they read explicit column indices (a row with
+ * more than 8 entries, more than 255 tuples, or TFLOWS_SELL_PATTERNS=0 when
+ * the topology was created).  Either way the products see the same columns
+ * in the same order. */
+int tflows_topology_patterns(tflows_topology *topo);
 
 /* Solve A x = b with device arrays in the topology's stored order: val
  * (nnz FP64), b (n), x (n, in/out: initial guess and solution), r_out (n,

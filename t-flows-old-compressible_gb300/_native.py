@@ -184,6 +184,7 @@ SIGNATURES = {
                                 ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "tflows_topology_destroy": ([_VP], None),
     "tflows_topology_transpose_map": ([_VP], _VP),
+    "tflows_topology_patterns": ([_VP], ctypes.c_int),
     "tflows_solve_device": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Options), _VP, _VP,
                              _VP, _VP, ctypes.c_int, ctypes.c_double, _VP,
                              ctypes.POINTER(Result)], ctypes.c_int),

@@ -246,6 +246,11 @@ class Topology:
     def handle(self):
         return self._h
 
+    @property
+    def patterns(self):
+        """Distinct column patterns the products read (0: explicit columns)."""
+        return int(lib().tflows_topology_patterns(self._h))
+
     def transpose_map(self):
         """Device pointer of the transposed-entry map (int32, nnz)."""
         p = lib().tflows_topology_transpose_map(self._h)

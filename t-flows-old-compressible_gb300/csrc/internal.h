@@ -30,6 +30,11 @@ struct DeviceTopology {
     int* col = nullptr;        // 0-based, nnz
     long long* soff = nullptr; // nslices + 1
     int* scol = nullptr;       // sell_len
+    // column patterns (see build_patterns): one id per row (32 * nslices),
+    // 8 offsets per pattern; null when the rows have too many patterns
+    unsigned char* spat = nullptr;
+    int* poff = nullptr;
+    int npat = 0;
     int* meta = nullptr;       // n: length | diag slot << 16
     int* perm_f = nullptr;
     int* perm_b = nullptr;

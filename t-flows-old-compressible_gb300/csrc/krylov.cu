@@ -138,13 +138,20 @@ int sweep_gate_on() {
     return v;
 }
 
+// Column patterns feed the FP64 products and the standalone product; the
+// FP32 inner solves keep explicit columns (measured at 256^3: the mixed CG
+// 2 % slower with patterns -- its persistent kernel is latency-bound at 50 %
+// occupancy and the table lookup lengthens each slice's dependency chain
+// more than the saved index bytes shorten it).
 template <typename T>
-Mat<T> make_mat(const DeviceTopology& t, const T* sval) {
+Mat<T> make_mat(const DeviceTopology& t, const T* sval, bool patterns = sizeof(T) == 8) {
     Mat<T> m;
     m.n = t.n;
     m.nslices = t.nslices;
     m.soff = t.soff;
     m.scol = t.scol;
+    m.spat = patterns ? t.spat : nullptr;
+    m.poff = patterns ? t.poff : nullptr;
     m.sval = sval;
     m.meta = t.meta;
     m.perm_f = t.perm_f;
@@ -414,7 +421,10 @@ cudaError_t prepare_mixed(const DeviceTopology& t, Workspace& ws, const SolveReq
 // each row's x gathered once, plus the vector passes of the schedule).
 double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevState& st) {
     const double sl = 8.0 * (t.nslices + 1);
-    const double spmv64 = (double)t.nnz * 12.0 + sl + 16.0 * t.n;
+    // column indices of one product: a pattern id per row (FP64 products of
+    // a topology with patterns), or 4 bytes per entry
+    const double idx64 = t.spat ? (double)t.n : 4.0 * t.nnz;
+    const double spmv64 = (double)t.nnz * 8.0 + idx64 + sl + 16.0 * t.n;
     const bool cgs = rq.method == 2;
     // One IC(0) apply: the off-diagonal factor entries (value + index) once,
     // the row metadata, D and the right-hand side read and the result written
@@ -761,7 +771,8 @@ cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, do
     cudaEventRecord(ws.ev0, s);
     for (int k = 0; k < std::max(1, repeat); ++k) {
         if (fp32) {
-            spmv_kernel<float, float><<<nb, kBlock, 0, s>>>(make_mat<float>(t, ws.sval32), x32, y32);
+            spmv_kernel<float, float><<<nb, kBlock, 0, s>>>(make_mat<float>(t, ws.sval32, true), x32,
+                                                            y32);
         } else {
             spmv_kernel<double, double><<<nb, kBlock, 0, s>>>(make_mat<double>(t, ws.sval64), x, y);
         }

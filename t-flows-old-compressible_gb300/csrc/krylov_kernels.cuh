@@ -48,6 +48,12 @@ struct Mat {
     int nslices;
     const long long* __restrict__ soff;  // nslices + 1 slice offsets (elements)
     const int* __restrict__ scol;        // SELL column indices, -1 = padding
+    // Column patterns (null when the topology has none): row i's entry t is
+    // at column i + poff[8 * spat[i] + t], absent where that offset is
+    // kNoCol (i + kNoCol < 0 for every row); the same columns as `scol`, in
+    // the same order, read as one byte per row instead of four per entry.
+    const unsigned char* __restrict__ spat;
+    const int* __restrict__ poff;
     const T* __restrict__ sval;          // SELL values
     const int* __restrict__ meta;        // per row: length | diag slot << 16
     const int* __restrict__ perm_f;      // forward level order, 32-padded, -1 pads
@@ -157,6 +163,36 @@ __device__ __forceinline__ double jacobi(double r, double d) { return r / d; }
 #endif
 __device__ __forceinline__ float jacobi(float r, float dinv) { return r * dinv; }
 
+// Offset marking an absent entry of a column pattern: patterns are built
+// only for fewer than 2^30 rows, so i + kNoCol is negative for every row.
+constexpr int kNoCol = -(1 << 30);
+
+// The first 8 column indices of row i = 32*s + lane of a slice of width
+// w <= 8 (negative where the row has no entry): from the row's column
+// pattern (two 16-byte loads of a table that stays in L1, one add per
+// entry) when the topology has patterns, else from the SELL column array.
+template <typename T>
+__device__ __forceinline__ void sell_cols8(const Mat<T>& m, int s, int lane, int w, long long b0,
+                                          int (&c)[8]) {
+    if (m.spat) {
+        const int i = s * kWarp + lane;
+        const int4* po = reinterpret_cast<const int4*>(m.poff) + 2 * (int)m.spat[i];
+        const int4 a = __ldg(po), b = __ldg(po + 1);
+        c[0] = i + a.x;
+        c[1] = i + a.y;
+        c[2] = i + a.z;
+        c[3] = i + a.w;
+        c[4] = i + b.x;
+        c[5] = i + b.y;
+        c[6] = i + b.z;
+        c[7] = i + b.w;
+    } else {
+        const int* cp = m.scol + b0 + lane;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) c[t] = t < w ? cp[32 * t] : -1;
+    }
+}
+
 // q_i = sum_j a_ij x_j over row i = 32*s + lane, left to right from 0.  Rows
 // of at most 8 stored entries (every hex or prism cell) take a fully
 // unrolled path: all index and value loads issue before the gathers.
@@ -170,11 +206,9 @@ __device__ __forceinline__ T sell_row(const Mat<T>& m, int s, int lane, const X*
     if (w <= 8) {
         int c[8];
         T v[8], xx[8];
+        sell_cols8(m, s, lane, w, b0, c);
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            c[t] = t < w ? cp[32 * t] : -1;
-            v[t] = t < w ? vp[32 * t] : T(0);
-        }
+        for (int t = 0; t < 8; ++t) v[t] = t < w ? vp[32 * t] : T(0);
 #pragma unroll
         for (int t = 0; t < 8; ++t) xx[t] = c[t] >= 0 ? T(xv[c[t]]) : T(0);
 #pragma unroll
@@ -210,11 +244,9 @@ __device__ __forceinline__ float sell_row_dir(const Mat<float>& m, int s, int la
     if (w <= 8) {
         int c[8];
         float v[8], zz[8], pp[8];
+        sell_cols8(m, s, lane, w, b0, c);
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            c[t] = t < w ? cp[32 * t] : -1;
-            v[t] = t < w ? vp[32 * t] : 0.f;
-        }
+        for (int t = 0; t < 8; ++t) v[t] = t < w ? vp[32 * t] : 0.f;
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
             zz[t] = c[t] >= 0 ? z[c[t]] : 0.f;
@@ -243,11 +275,9 @@ __device__ __forceinline__ T sell_resid_row(const Mat<T>& m, int s, int lane, T 
     if (w <= 8) {
         int c[8];
         T v[8], xx[8];
+        sell_cols8(m, s, lane, w, b0, c);
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            c[t] = t < w ? cp[32 * t] : -1;
-            v[t] = t < w ? vp[32 * t] : T(0);
-        }
+        for (int t = 0; t < 8; ++t) v[t] = t < w ? vp[32 * t] : T(0);
 #pragma unroll
         for (int t = 0; t < 8; ++t) xx[t] = c[t] >= 0 ? T(xv[c[t]]) : T(0);
 #pragma unroll

@@ -9,10 +9,12 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -135,10 +137,59 @@ cudaError_t upload(T** dst, const T* src, size_t count) {
 
 void free_topology_arrays(DeviceTopology& t) {
     for (void* p : {(void*)t.rowptr, (void*)t.col, (void*)t.soff, (void*)t.scol, (void*)t.meta,
-                    (void*)t.perm_f, (void*)t.perm_b, (void*)t.tpos})
+                    (void*)t.perm_f, (void*)t.perm_b, (void*)t.tpos, (void*)t.spat,
+                    (void*)t.poff})
         if (p) cudaFree(p);
     t.rowptr = t.col = t.scol = t.meta = t.perm_f = t.perm_b = t.tpos = nullptr;
     t.soff = nullptr;
+    t.spat = nullptr;
+    t.poff = nullptr;
+    t.npat = 0;
+}
+
+// Column patterns: when every row has at most 8 stored entries and the rows'
+// offset tuples (column - row, in stored order) take at most 255 distinct
+// values -- cells of a structured or block-structured mesh repeat a few
+// stencils -- each row stores a one-byte pattern id and the products read
+// the offsets from an 8-int table, instead of 4 bytes of column index per
+// entry.  Turned off by TFLOWS_SELL_PATTERNS=0.
+cudaError_t build_patterns(DeviceTopology& t) {
+    const char* env = std::getenv("TFLOWS_SELL_PATTERNS");
+    if ((env && *env && std::atoi(env) == 0) || t.max_len > 8 || t.n <= 0 || t.n >= (1 << 30))
+        return cudaSuccess;
+    constexpr int kNoColHost = -(1 << 30);  // i + kNoColHost < 0 for every row
+    std::map<std::array<int, 8>, int> ids;
+    std::vector<std::array<int, 8>> table;
+    std::vector<unsigned char> spat((size_t)t.nslices * 32);
+    auto id_of = [&](const std::array<int, 8>& key) -> int {
+        auto it = ids.find(key);
+        if (it != ids.end()) return it->second;
+        if (table.size() >= 255) return -1;
+        ids.emplace(key, (int)table.size());
+        table.push_back(key);
+        return (int)table.size() - 1;
+    };
+    for (size_t i = 0; i < spat.size(); ++i) {
+        std::array<int, 8> key;
+        key.fill(kNoColHost);
+        if ((int)i < t.n) {
+            const int b = t.h_rowptr[i], e = t.h_rowptr[i + 1];
+            for (int j = b; j < e; ++j) {
+                key[j - b] = t.h_col[j] - (int)i;  // |offset| < n < 2^30
+            }
+        }
+        const int id = id_of(key);
+        if (id < 0) return cudaSuccess;  // too many patterns: explicit columns
+        spat[i] = (unsigned char)id;
+    }
+    std::vector<int> poff(table.size() * 8);
+    for (size_t p = 0; p < table.size(); ++p)
+        for (int k = 0; k < 8; ++k) poff[8 * p + k] = table[p][k];
+    cudaError_t e;
+    if ((e = upload(&t.spat, spat.data(), spat.size())) != cudaSuccess) return e;
+    if ((e = upload(&t.poff, poff.data(), poff.size())) != cudaSuccess) return e;
+    t.npat = (int)table.size();
+    return cudaSuccess;
 }
 
 // SELL-32 layout: slice s holds rows 32s..32s+31, width = longest row.
@@ -167,7 +218,7 @@ cudaError_t build_device(DeviceTopology& t) {
     if ((e = upload(&t.soff, soff.data(), soff.size())) != cudaSuccess) return e;
     if ((e = upload(&t.scol, scol.data(), scol.size())) != cudaSuccess) return e;
     if ((e = upload(&t.meta, meta.data(), meta.size())) != cudaSuccess) return e;
-    return cudaSuccess;
+    return build_patterns(t);
 }
 
 // Wavefront levels of the forward (lower, in row order) and backward (upper,
@@ -784,6 +835,8 @@ void tflows_topology_destroy(tflows_topology* topo) {
     destroy_topo(topo);
     delete topo;
 }
+
+int tflows_topology_patterns(tflows_topology* topo) { return topo ? topo->t.npat : 0; }
 
 const int* tflows_topology_transpose_map(tflows_topology* topo) {
     if (!topo) return nullptr;
