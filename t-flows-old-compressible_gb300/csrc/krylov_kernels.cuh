@@ -242,11 +242,15 @@ __device__ __forceinline__ float sell_row_dir(const Mat<float>& m, int s, int la
     const float* vp = m.sval + b0 + lane;
     float acc = 0.f;
     if (w <= 8) {
+        // the FP32 inner solves read explicit columns (their matrices carry no
+        // patterns), so this loop has no pattern branch
         int c[8];
         float v[8], zz[8], pp[8];
-        sell_cols8(m, s, lane, w, b0, c);
 #pragma unroll
-        for (int t = 0; t < 8; ++t) v[t] = t < w ? vp[32 * t] : 0.f;
+        for (int t = 0; t < 8; ++t) {
+            c[t] = t < w ? cp[32 * t] : -1;
+            v[t] = t < w ? vp[32 * t] : 0.f;
+        }
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
             zz[t] = c[t] >= 0 ? z[c[t]] : 0.f;
