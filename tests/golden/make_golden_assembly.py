@@ -8,7 +8,8 @@ loop, the density-derivative source and the removal of the volume-weighted
 mean of b -- wraps them in a subroutine, translates it with
 fortran_subset.py (derived-type components such as ``Rho % n`` become plain
 names) and runs it on small perturbed boxes whose boundary cells carry every
-boundary type of Library/allp_mod.f90, with Nmat = 1 and 2.  Writes
+boundary type of Library/allp_mod.f90, with Nmat = 1 and 2, and on a box with
+one face repeated (two faces joining the same cells).  Writes
 assembly_*.npz: the inputs and Aval, b, Abou, Flux, errmax.
 
 Run:  python tests/golden/make_golden_assembly.py [/path/to/T-FlowS]
@@ -86,9 +87,33 @@ def run_reference(root, msh, fields, typebc, nmat, dt):
     return arr(M.aval), arr(M.b), arr(M.abou)[:NbC], arr(M.flux), float(M.errmax)
 
 
-def case(root, name, shape, seed, nmat):
+def duplicate_face(msh, frac=0.5):
+    """The box with one interior face repeated right after itself (two faces
+    joining the same two cells, as a split face of a polyhedral mesh gives),
+    the second one with a 1.5 times larger Sx so that face order shows.  The
+    layout is rebuilt as Process/TopolM.f90 builds it (the C restatement in
+    oracle/): the pair's row holds the neighbour twice and both faces get the
+    last of its positions."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import oracle
+    inner = np.nonzero(msh["SideC"][:, 2] > 0)[0]
+    dup = int(inner[int(len(inner) * frac)])
+    order = np.r_[np.arange(dup + 1), dup, np.arange(dup + 1, msh["NS"])]
+    out = dict(msh)
+    for k in ("SideC", "Sx", "Sy", "Sz", "Dx", "Dy", "Dz", "f"):
+        out[k] = np.ascontiguousarray(msh[k][order])
+    out["Sx"][dup + 1] *= 1.5
+    out["NS"] = msh["NS"] + 1
+    Acol, Arow, Adia, sid = oracle.topolm(msh["NC"], out["SideC"][:, 1:])
+    out.update(Acol=Acol, Arow=Arow, Adia=Adia, SidAij=sid)
+    return out
+
+
+def case(root, name, shape, seed, nmat, dup=False):
     mesh = _mesh()
     msh = mesh.box_faces(*shape, perturb=0.2, seed=seed)
+    if dup:
+        msh = duplicate_face(msh)
     NC, NbC = msh["NC"], msh["NbC"]
     rng = np.random.default_rng(seed + 1000)
     n = NbC + NC + 1
@@ -125,6 +150,7 @@ def main():
     case(root, "box533_nmat1", (5, 3, 3), 3, 1)
     case(root, "box444_nmat2", (4, 4, 4), 4, 2)
     case(root, "box271_nmat1", (2, 7, 1), 5, 1)
+    case(root, "box433_dupface", (4, 3, 3), 6, 1, dup=True)
 
 
 if __name__ == "__main__":

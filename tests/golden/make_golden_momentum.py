@@ -16,7 +16,8 @@ call the test-problem functions of Moin_Problem_Mod, so `Ui % source` is an
 input here.  The lines are translated with fortran_subset.py and run on small
 perturbed boxes whose boundary cells carry every boundary type of
 Library/allp_mod.f90, for every convection scheme of Process/IniPar.f90 and
-each time-discretisation option.  Writes momentum_*.npz: the inputs and
+each time-discretisation option, and on a box with one face repeated (two
+faces joining the same cells).  Writes momentum_*.npz: the inputs and
 Aval, b, Abou, Asave.
 
 Run:  python tests/golden/make_golden_momentum.py [/path/to/T-FlowS]
@@ -34,7 +35,7 @@ sys.path.insert(0, HERE)
 
 from fortran_subset import FArr, Module, load_subroutines  # noqa: E402
 from make_golden import _mesh  # noqa: E402
-from make_golden_assembly import F2  # noqa: E402
+from make_golden_assembly import F2, duplicate_face  # noqa: E402
 
 # Library/allp_mod.f90:16-24 and Process/IniPar.f90:22-49
 BC = {"inflow": 1, "wall": 2, "outflow": 3, "symmetry": 4, "convect": 5, "wallfl": 6,
@@ -210,9 +211,11 @@ def make_inputs(msh, seed, nmat, blend, blend_tem, var, convec=3, cross=3, diffu
     return inp
 
 
-def case(root, name, shape, seed, nmat, blend, blend_tem, var, **kw):
+def case(root, name, shape, seed, nmat, blend, blend_tem, var, dup=False, **kw):
     mesh = _mesh()
     msh = mesh.box_faces(*shape, perturb=0.2, seed=seed)
+    if dup:
+        msh = duplicate_face(msh)
     inp = make_inputs(msh, seed, nmat, blend, blend_tem, var, **kw)
     res = run_reference(root, msh, inp)
     out = dict(NC=msh["NC"], NbC=msh["NbC"], NS=msh["NS"], NONZ=int(msh["Acol"][-1]),
@@ -243,6 +246,8 @@ def main():
     # Crank-Nicolson diffusion flag, explicit terms off, no inertial term
     case(root, "box271_cn", (2, 7, 1), 5, 1, [C["quick"]], [C["no"]], 3, convec=C["ab"],
          cross=C["cn"], diffus=C["cn"], inert=C["ab"])
+    # two faces joining the same two cells (one off-diagonal position each way)
+    case(root, "box433_dupface_smart", (4, 3, 3), 6, 1, [C["smart"]], [C["yes"]], 1, dup=True)
 
 
 if __name__ == "__main__":
