@@ -169,6 +169,8 @@ cudaError_t build_patterns(DeviceTopology& t) {
         table.push_back(key);
         return (int)table.size() - 1;
     };
+    std::array<int, 8> last;
+    int last_id = -1;
     for (size_t i = 0; i < spat.size(); ++i) {
         std::array<int, 8> key;
         key.fill(kNoColHost);
@@ -178,9 +180,12 @@ cudaError_t build_patterns(DeviceTopology& t) {
                 key[j - b] = t.h_col[j] - (int)i;  // |offset| < n < 2^30
             }
         }
-        const int id = id_of(key);
+        // neighbouring rows mostly share a stencil: look up only on a change
+        const int id = last_id >= 0 && key == last ? last_id : id_of(key);
         if (id < 0) return cudaSuccess;  // too many patterns: explicit columns
         spat[i] = (unsigned char)id;
+        last = key;
+        last_id = id;
     }
     std::vector<int> poff(table.size() * 8);
     for (size_t p = 0; p < table.size(); ++p)
