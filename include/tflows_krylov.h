@@ -308,7 +308,9 @@ int tflows_topolm(int NC, int NS, const int *SideC, int *Acol, int *Arow,
  * SideC(0:2,NS) and SidAij(2,NS) as the reference holds them (column-major),
  * Adia(NC) 1-based, TypeBC(-NbC:NC) and volume(-NbC:NC) passed at their
  * element -NbC, face geometry Sx..Sz, Dx..Dz, f(1:NS) (Library/GeoLoa.f90).
- * Every index is checked here; bad ones give TFLOWS_BAD_INPUT. */
+ * Every index is checked here; bad ones give TFLOWS_BAD_INPUT.  An object
+ * keeps per-call scratch on the device, so it serves one assembly call at a
+ * time (calls on different objects may overlap). */
 typedef struct tflows_assembly tflows_assembly;
 int tflows_assembly_create(tflows_assembly **out, int NC, int NbC, int NS,
                            int NONZ, const int *SideC, const int *SidAij,
