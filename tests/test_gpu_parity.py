@@ -21,7 +21,7 @@ mesh = tflows.mesh
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 SOLVER_CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
                       if not os.path.basename(p).startswith(("prec1_resid", "assembly_",
-                                                                 "momentum_")))
+                                                                 "momentum_", "topolm_")))
 PR_CASES = sorted(glob.glob(os.path.join(GOLDEN, "prec1_resid_*.npz")))
 REL = 1e-8
 

@@ -4,7 +4,10 @@ The fixtures in tests/golden/ come from executing Process/{CG,BiCG,CGS,
 Prec1,Resid}.f90 statement by statement (tests/golden/make_golden.py); the C
 restatement in oracle/ must reproduce every output bit for bit, including
 the module state carried between calls and the early-exit and
-non-convergence conventions.
+non-convergence conventions.  The assembly (CalcPS, NewUVW with ConvScheme
+and CalMinMax) and layout (TopolM) fixtures come from the same kind of
+execution of those files (make_golden_assembly.py, make_golden_momentum.py,
+make_golden_topolm.py).
 """
 import glob
 import os
@@ -17,7 +20,7 @@ import oracle
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 SOLVER_CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
                       if not os.path.basename(p).startswith(("prec1_resid", "assembly_",
-                                                                 "momentum_")))
+                                                                 "momentum_", "topolm_")))
 PR_CASES = sorted(glob.glob(os.path.join(GOLDEN, "prec1_resid_*.npz")))
 
 
@@ -153,3 +156,27 @@ def test_momentum_oracle_rejects_undefined_blending_and_materials():
     mat[int(g["NbC"]) + 3] = 3
     *_, st = momentum_oracle_case(g, material=mat)
     assert st == 2
+
+
+TOPOLM_CASES = sorted(glob.glob(os.path.join(GOLDEN, "topolm_*.npz")))
+
+
+@pytest.mark.parametrize("path", TOPOLM_CASES, ids=lambda p: os.path.basename(p)[:-4])
+def test_topolm_layouts_match_reference_source(path):
+    """Process/TopolM.f90 executed from the reference source (its ISort call
+    replaced by another sort of the same integers) gives Acol, Arow, Adia
+    and SidAij; the oracle's restatement and the library's tflows_topolm
+    (host code) reproduce them exactly -- including two faces joining the
+    same cells, where the row holds the neighbour twice and both faces get
+    its last position.  (The box mesh builder equals tflows_topolm on boxes,
+    tests/test_mesh_files.py.)"""
+    from conftest import tflows
+    g = np.load(path)
+    NC, SideC = int(g["NC"]), g["SideC"]
+    oA, oR, oD, oS = oracle.topolm(NC, SideC[:, 1:])
+    lA, lR, lD, lS = tflows.topolm(NC, SideC)
+    for A, R, D, S in ((oA, oR, oD, oS), (lA, lR, lD, lS)):
+        assert np.array_equal(A, g["Acol"]) and np.array_equal(R, g["Arow"])
+        assert np.array_equal(D, g["Adia"])
+        assert np.array_equal(np.asarray(S).reshape(-1, 2), g["SidAij"])
+    assert int(g["NONZERO"]) == int(g["Acol"][-1])
