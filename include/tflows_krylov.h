@@ -413,7 +413,13 @@ int tflows_newuvw_assemble_device(tflows_assembly *a, const tflows_newuvw_params
  * to 262144 rows (larger: TFLOWS_BAD_INPUT; prec 2: TFLOWS_UNSUPPORTED).
  * All calls share that array, so calls that overlap on the GPU race.  The
  * first call on a device looks up the array's address (cudaGetSymbolAddress)
- * and should come before any stream capture.  The pattern is not checked.
+ * and should come before any stream capture; the lookup is repeated after
+ * the device's context has been replaced (cudaDeviceReset).  Every call
+ * waits for `stream` to finish before it returns, to read its status.  The
+ * pattern is checked on the device before use: row pointers starting at 0
+ * and never decreasing, columns in [0, n), with prec 1 diagonal positions
+ * inside their rows; otherwise TFLOWS_BAD_INPUT and x, r_out untouched.
+ * rowptr[n] must not exceed the length of col and val (not checkable here).
  * Returns the status; *iterations, *ini_res, *fin_res as in tflows_cg (on the
  * ||b|| < tol exit *ini_res and *fin_res are left as they were). */
 int tflows_cg_noalloc(int n, const int *rowptr, const int *col,

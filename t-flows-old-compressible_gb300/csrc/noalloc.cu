@@ -19,9 +19,18 @@
 //     race on it and must not be issued;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current); make that first call
-//     before capturing any stream.
+//     before capturing any stream.  The lookup is repeated when the device's
+//     context has changed since (after cudaDeviceReset, for example);
+//   * every call waits for its stream to finish before it returns (it reads
+//     the status record back);
+//   * the pattern is checked on the device (row pointers from 0, never
+//     decreasing; columns in [0, n); diagonal positions inside their rows):
+//     TFLOWS_BAD_INPUT, with nothing written to x or r_out.
 #include "../../include/tflows_krylov.h"
 #include "device_common.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -72,8 +81,31 @@ __global__ void __launch_bounds__(kNaBlock) noalloc_cg_kernel(NaParams P) {
     int exit_kind = EXIT_ABORT, iterations = 0;
     double ini = 0.0, err = 0.0;
 
+    // The caller's pattern, checked before any vector is indexed through it:
+    // row pointers start at 0 and never decrease, every column lies in
+    // [0, n), and (prec 1) every diagonal position lies inside its row.  A
+    // bad row raises BAD_INPUT and skips the loads that depend on it; the
+    // barrier then makes the flag visible to every block before the first
+    // gather.  (rowptr[n] itself must not exceed the length of col and val:
+    // the call has no way to know that length.)
+    for (int i = tid; i < n; i += nt) {
+        const int j0 = P.rowptr[i], j1 = P.rowptr[i + 1];
+        bool bad = j0 < 0 || j1 < j0 || (i == 0 && j0 != 0);
+        for (int j = j0; !bad && j < j1; ++j) {
+            const int c = P.col[j];
+            bad = c < 0 || c >= n;
+        }
+        if (!bad && prec == 1) {
+            const int d = P.diag[i];
+            bad = d < j0 || d >= j1;
+        }
+        if (bad) raise_abort(P.ctl, ST_BAD_INPUT, 95);
+    }
+    double a1[1];  // (declared before the jump, initialised after it)
+    if (!grid_sync(g, 96)) goto done;
+
     // Prec1 (diag or 1), r = b, ||b||
-    double a1[1] = {0.0};
+    a1[0] = 0.0;
     for (int i = tid; i < n; i += nt) {
         P.D[i] = prec == 1 ? P.val[P.diag[i]] : 1.0;
         const double bi = P.b[i];
@@ -194,9 +226,44 @@ done:
     }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array, looked up once per device and
+// remembered together with the identity of the context it was looked up in:
+// after cudaDeviceReset (or the release of the primary context) the device
+// gets a new context with a new copy of the array, and the address is looked
+// up again.  The context identity comes from the driver (cuCtxGetCurrent,
+// cuCtxGetId), reached through the runtime's entry-point query so the
+// library needs no link against libcuda.
+struct AddrEntry {
+    unsigned long long ctx_id;  // 0: not looked up yet
+    void* ptr;
+};
 std::mutex g_addr_mu;
-void* g_addr[64] = {};
+AddrEntry g_addr[64] = {};
+PFN_cuCtxGetCurrent_v4000 g_ctx_current = nullptr;
+PFN_cuCtxGetId_v12000 g_ctx_id = nullptr;
+bool g_ctx_fns_tried = false;
+
+// Identity of the calling thread's current context (0 when there is none or
+// the driver cannot tell).  Call with g_addr_mu held.
+unsigned long long current_context_id() {
+    if (!g_ctx_fns_tried) {
+        g_ctx_fns_tried = true;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void**)&g_ctx_current, 4000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            g_ctx_current = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", (void**)&g_ctx_id, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            g_ctx_id = nullptr;
+    }
+    if (!g_ctx_current || !g_ctx_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx || g_ctx_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 }  // namespace
 }  // namespace tflows
@@ -215,14 +282,22 @@ extern "C" int tflows_cg_noalloc(int n, const int* rowptr, const int* col, const
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TFLOWS_NO_DEVICE;
     unsigned char* base = nullptr;
     {
+        // Set-up, once per device (and again after that device's context
+        // was replaced), with the device current: the host-side name
+        // g_noalloc_scratch is not a device address, so the kernel gets the
+        // address the runtime reports for it.
         std::lock_guard<std::mutex> lk(g_addr_mu);
-        if (!g_addr[dev]) {
+        AddrEntry& e = g_addr[dev];
+        const unsigned long long id = current_context_id();
+        if (!e.ptr || id == 0 || id != e.ctx_id) {
             void* ptr = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-            if (e != cudaSuccess || !ptr) return TFLOWS_CUDA_ERROR;
-            g_addr[dev] = ptr;
+            if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr)
+                return TFLOWS_CUDA_ERROR;
+            e.ptr = ptr;
+            // the lookup above made the runtime's context current if none was
+            e.ctx_id = id != 0 ? id : current_context_id();
         }
-        base = static_cast<unsigned char*>(g_addr[dev]);
+        base = static_cast<unsigned char*>(e.ptr);
     }
     NaParams P;
     P.n = n;

@@ -1,7 +1,7 @@
 """Generate the golden fixtures by executing the reference's own source text.
 
 Reads Process/{CG,BiCG,CGS,Prec1,Resid}.f90 from a T-FlowS checkout (default
-/root/reference, or the path given as the first argument), translates them
+the path given as the first argument or in TFLOWS_REFERENCE), translates them
 with fortran_subset.py, runs a fixed list of small cases through the
 translated subroutines and writes one .npz per case into this directory:
 inputs (the Fortran-layout arrays and scalars) and outputs (x, r1, niter,
@@ -200,5 +200,15 @@ def main(root):
         print(f"prec1_resid_{key}")
 
 
+
+def reference_root():
+    """The T-FlowS checkout to read: the first argument, else the
+    TFLOWS_REFERENCE environment variable; one of them is required."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TFLOWS_REFERENCE")
+    if not root:
+        sys.exit(f"usage: {os.path.basename(sys.argv[0])} PATH_TO_T-FLOWS_CHECKOUT "
+                 "(or set TFLOWS_REFERENCE)")
+    return root
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(reference_root())

@@ -2,7 +2,7 @@
 own source text.
 
 Extracts Process/CalcPS.f90 lines 69-202 of a T-FlowS checkout (default
-/root/reference, or the path given as the first argument) -- the face loop
+the path given as the first argument or in TFLOWS_REFERENCE) -- the face loop
 that fills Aval through SidAij/Adia, Abou, the face fluxes and b, the errmax
 loop, the density-derivative source and the removal of the volume-weighted
 mean of b -- wraps them in a subroutine, translates it with
@@ -146,12 +146,22 @@ def case(root, name, shape, seed, nmat, dup=False):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = reference_root()
     case(root, "box533_nmat1", (5, 3, 3), 3, 1)
     case(root, "box444_nmat2", (4, 4, 4), 4, 2)
     case(root, "box271_nmat1", (2, 7, 1), 5, 1)
     case(root, "box433_dupface", (4, 3, 3), 6, 1, dup=True)
 
+
+
+def reference_root():
+    """The T-FlowS checkout to read: the first argument, else the
+    TFLOWS_REFERENCE environment variable; one of them is required."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TFLOWS_REFERENCE")
+    if not root:
+        sys.exit(f"usage: {os.path.basename(sys.argv[0])} PATH_TO_T-FLOWS_CHECKOUT "
+                 "(or set TFLOWS_REFERENCE)")
+    return root
 
 if __name__ == "__main__":
     main()

@@ -6,8 +6,8 @@ blends, the zeroing of the convective and cross-diffusive sums) and 200-499
 (the convection face loop, the diffusion face loop that fills Aval through
 Adia/SidAij, b and Abou, the cross-diffusion, inertial, pressure and
 under-relaxation terms), together with the whole of Process/ConvScheme.f90
-and Process/CalMinMax.f90 of a T-FlowS checkout (default /root/reference, or
-the path given as the first argument).  Mechanical rewrites only: derived-type
+and Process/CalMinMax.f90 of a T-FlowS checkout (the path given as the
+first argument or in TFLOWS_REFERENCE).  Mechanical rewrites only: derived-type
 components such as ``Ui % C`` become plain names, the `select case
 (Moin_Problem())` inside the diffusion loop becomes an if/else on the same
 value, and each statement on the array section ``(1:NC)`` becomes the
@@ -231,7 +231,7 @@ def case(root, name, shape, seed, nmat, blend, blend_tem, var, dup=False, **kw):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = reference_root()
     C = CODES
     # no blending: central convection explicit, diffusion implicit
     case(root, "box533_no", (5, 3, 3), 3, 1, [C["no"]], [C["no"]], 1)
@@ -249,6 +249,16 @@ def main():
     # two faces joining the same two cells (one off-diagonal position each way)
     case(root, "box433_dupface_smart", (4, 3, 3), 6, 1, [C["smart"]], [C["yes"]], 1, dup=True)
 
+
+
+def reference_root():
+    """The T-FlowS checkout to read: the first argument, else the
+    TFLOWS_REFERENCE environment variable; one of them is required."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TFLOWS_REFERENCE")
+    if not root:
+        sys.exit(f"usage: {os.path.basename(sys.argv[0])} PATH_TO_T-FLOWS_CHECKOUT "
+                 "(or set TFLOWS_REFERENCE)")
+    return root
 
 if __name__ == "__main__":
     main()

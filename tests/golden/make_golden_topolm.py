@@ -3,7 +3,7 @@
 Extracts the body of Process/TopolM.f90 (stencil widths from SideC, the row
 pointers Acol, the columns Arow sorted per row, the diagonal positions Adia
 and the face positions SidAij) of a T-FlowS checkout (default
-/root/reference, or the path given as the first argument) and executes it
+the path given as the first argument or in TFLOWS_REFERENCE) and executes it
 statement by statement with fortran_subset.py.  Mechanical rewrites only:
 the allocations, the progress messages and the deallocation are dropped
 (the arrays are provided here, zeroed), and the call to the library sort
@@ -118,11 +118,21 @@ def case(root, name, shape, seed, dup=False):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = reference_root()
     case(root, "box543", (5, 4, 3), 1)
     case(root, "box271", (2, 7, 1), 2)
     case(root, "box443_dupfaces", (4, 4, 3), 3, dup=True)
 
+
+
+def reference_root():
+    """The T-FlowS checkout to read: the first argument, else the
+    TFLOWS_REFERENCE environment variable; one of them is required."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TFLOWS_REFERENCE")
+    if not root:
+        sys.exit(f"usage: {os.path.basename(sys.argv[0])} PATH_TO_T-FLOWS_CHECKOUT "
+                 "(or set TFLOWS_REFERENCE)")
+    return root
 
 if __name__ == "__main__":
     main()
