@@ -436,6 +436,57 @@ def cfg1_latency(pkg, dev, reps=20):
     return out
 
 
+def ic_block(pkg, dev, n=128, iters=0, precisions=("fp64", "fp64_fma", "mixed"), tiled=(0, 1),
+             reps=2):
+    """IC(0)-preconditioned CG on the config-3 variable-density pressure
+    system at n^3: per precision and per sweep kind (tiled / level-ordered),
+    the time per iteration of the persistent solve (capped at `iters`
+    iterations, 0 = to the tolerance) and one standalone IC apply (pivots +
+    forward + backward, tflows_ic_apply_device) for the FP64 builds."""
+    import torch
+    s = make_workload(pkg, "cfg3", n)
+    topo = pkg.Topology.from_system(s)
+    val = torch.from_numpy(s.A[:-1].copy()).to(dev)
+    b = torch.from_numpy(s.b.copy()).to(dev)
+    x = torch.zeros(s.N, dtype=torch.float64, device=dev)
+    z = torch.empty_like(x)
+    maxit = iters if iters > 0 else 20000
+    mode = {"fp64": pkg.FP64, "fp64_fma": pkg.FP64_FMA, "mixed": pkg.MIXED}
+    out = {"workload": f"{s.name}: CG + IC(0), tol 1e-8*||b|| (absolute), x0=0"
+                       + (f", capped at {iters} iterations" if iters else ""), "n": s.N}
+    for label in precisions:
+        for t in tiled:
+            kw = {"ic_bf16": 1} if label == "mixed" else {}
+            opts = pkg.options(precision=mode[label], ic_tiled=t, **kw)
+            x.zero_()
+            topo.solve(val, b, x, "cg", 2, maxit, s.tol, opts=opts, raise_on_error=False)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                x.zero_()
+                r = topo.solve(val, b, x, "cg", 2, maxit, s.tol, opts=opts, raise_on_error=False)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            it = max(1, r["inner_iterations"] if label == "mixed" else r["iterations"])
+            rec = {"ms": ms, "iterations": it, "us_per_iteration": 1e3 * ms / it,
+                   "status": r["status"], "gbs": r["bytes"] / r["seconds"] / 1e9,
+                   "refinements": r["refinements"]}
+            if label != "mixed":
+                topo.ic_apply(val, b, z, opts=opts)
+                torch.cuda.synchronize()
+                e0.record()
+                for _ in range(reps):
+                    topo.ic_apply(val, b, z, opts=opts)
+                e1.record()
+                torch.cuda.synchronize()
+                rec["pivots_plus_apply_ms"] = e0.elapsed_time(e1) / reps
+            out[f"{label}_{'tiled' if t else 'level'}"] = rec
+    topo.close()
+    return out
+
+
 def adjoint_cfg5(pkg, dev, reps=3):
     """Config 5: 64^3 variable-density pressure assembled differentiably from
     its float32 face coefficients, loss 0.5||x - x_t||^2, one forward solve
@@ -712,9 +763,16 @@ def main():
                     help="fixed launch shape (256 threads, one slice per warp)")
     ap.add_argument("--ic-compare-scale", type=int, default=256,
                     help="edge of the IC mixed-vs-FP64 comparison (0 = skip)")
-    ap.add_argument("--block", default=None, choices=["calcps", "newuvw", "cfg1"],
+    ap.add_argument("--block", default=None, choices=["calcps", "newuvw", "cfg1", "ic"],
                     help="run only this block (an assembly on a --scale^3 box, default 128, "
-                         "or the config-1 latency block), print its JSON and exit")
+                         "the config-1 latency block, or IC(0) CG on the config-3 system at "
+                         "--scale^3), print its JSON and exit")
+    ap.add_argument("--ic-iters", type=int, default=0,
+                    help="--block ic: iteration cap of each solve (0 = to the tolerance)")
+    ap.add_argument("--ic-tiled", type=int, default=-1,
+                    help="--block ic: 1 tiled sweeps only, 0 level-ordered only, -1 both")
+    ap.add_argument("--ic-precisions", default="fp64,fp64_fma,mixed",
+                    help="--block ic: comma-separated precisions to time")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -728,6 +786,12 @@ def main():
         dev = torch.device("cuda", 0)
         if args.block == "cfg1":
             print(json.dumps(cfg1_latency(pkg, dev)), flush=True)
+            return
+        if args.block == "ic":
+            tiled = (0, 1) if args.ic_tiled < 0 else (args.ic_tiled,)
+            print(json.dumps(ic_block(pkg, dev, n=args.scale or 128, iters=args.ic_iters,
+                                      precisions=tuple(args.ic_precisions.split(",")),
+                                      tiled=tiled, reps=1 if args.ic_iters else 2)), flush=True)
             return
         fn = {"calcps": assembly_block, "newuvw": momentum_block}[args.block]
         print(json.dumps(fn(pkg, dev, n=args.scale or 128)), flush=True)

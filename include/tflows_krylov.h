@@ -66,8 +66,9 @@ typedef struct tflows_options {
                             refinement (default, always for CGS); 0 = CG keeps
                             its search direction across refinements
                             (reliable updates)                              */
-    int ic_sweeps;       /* mixed + prec 2: 0 = exact triangular sweeps,
-                            k > 0 = k Jacobi sweeps per triangle            */
+    int ic_sweeps;       /* prec 2 in mixed or TFLOWS_FP64_FMA solves: 0 =
+                            exact triangular sweeps, k > 0 = k Jacobi sweeps
+                            per triangle                                    */
     int ic_bf16;         /* mixed + prec 2: IC off-diagonals stored in BF16 */
     double timeout_s;    /* limit for any single device-side wait           */
     int block_size;      /* threads per block (multiple of 32, 64..512),
@@ -89,6 +90,14 @@ typedef struct tflows_options {
                             representative cell until it is ready, 0 = every
                             lane polls every input, -1 = the default (on,
                             TFLOWS_SWEEP_GATE=0 turns it off)              */
+    int ic_tiled;        /* exact IC(0) on a box-numbered pattern (row =
+                            x + nx (y + ny z), 7-point TopolM rows): 1 =
+                            tiled sweeps (block-local wavefront steps, bulk
+                            copies into shared memory), 0 = level-ordered
+                            sweeps, -1 = the default (tiled, TFLOWS_IC_TILED=0
+                            turns it off).  In reference arithmetic both give
+                            the same apply bit for bit.  Other patterns always
+                            use the level sweeps                            */
 } tflows_options;
 
 typedef struct tflows_result {
@@ -270,6 +279,17 @@ int tflows_pattern_outer(tflows_topology *topo, const double *lambda,
 /* Standalone compressed-row product y = A x on device arrays (FP64 or, with
  * fp32 = 1, values/vectors converted to FP32 on the fly).  For tests and
  * bandwidth measurement; returns the kernel time in seconds through *sec. */
+/* The IC(0) preconditioner of Process/Prec1.f90:51-59 and CG.f90:124-166 as
+ * an operator on device arrays: the pivots D, then z = M^-1 r with the
+ * reference's forward sweep, TINY middle step and backward sweep, in FP64
+ * (opt->precision TFLOWS_FP64: reference arithmetic, bit-identical per row to
+ * the sequential loops; TFLOWS_FP64_FMA: contracted).  opt->ic_tiled picks
+ * the tiled or the level-ordered sweeps; NULL opt = defaults.  Synchronous
+ * on `stream`; *res (may be NULL) gets the status and the device time. */
+int tflows_ic_apply_device(tflows_topology *topo, const tflows_options *opt,
+                           const double *val, const double *r, double *z,
+                           void *stream, tflows_result *res);
+
 int tflows_spmv_device(tflows_topology *topo, const double *val,
                        const double *x, double *y, int repeat, int fp32,
                        void *stream, double *sec);

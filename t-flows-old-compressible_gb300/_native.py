@@ -100,7 +100,8 @@ class Options(ctypes.Structure):
                 ("block_size", ctypes.c_int), ("grid_blocks", ctypes.c_int),
                 ("device", ctypes.c_int), ("inject_stall", ctypes.c_int),
                 ("autotune", ctypes.c_int), ("rows_per_warp", ctypes.c_int),
-                ("sweep_warps", ctypes.c_int), ("sweep_gate", ctypes.c_int)]
+                ("sweep_warps", ctypes.c_int), ("sweep_gate", ctypes.c_int),
+                ("ic_tiled", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -191,6 +192,8 @@ SIGNATURES = {
     "tflows_solve_batched_device": ([ctypes.c_int, _VP, _VP, _VP, ctypes.POINTER(Options), _VP, _VP,
                                      _VP, _VP, _VP, _VP, ctypes.POINTER(Result)], ctypes.c_int),
     "tflows_pattern_outer": ([_VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+    "tflows_ic_apply_device": ([_VP, ctypes.POINTER(Options), _VP, _VP, _VP, _VP,
+                                ctypes.POINTER(Result)], ctypes.c_int),
     "tflows_spmv_device": ([_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int, _VP,
                             ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
     "tflows_plan_create": ([ctypes.POINTER(_VP), ctypes.c_int, _VP, _VP, _VP,

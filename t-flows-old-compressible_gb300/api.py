@@ -289,6 +289,20 @@ class Topology:
             raise SolverError(st, last_error())
         return out.as_dict()
 
+    def ic_apply(self, val, r, z, opts=None):
+        """IC(0) pivots and z = M^-1 r (tflows_ic_apply_device) on torch CUDA
+        float64 tensors; returns the result record as a dict."""
+        for t in (val, r, z):
+            if not (t.is_cuda and t.dtype.itemsize == 8 and t.is_contiguous()):
+                raise TypeError("val, r, z must be contiguous CUDA float64 tensors")
+        res = _native.Result()
+        st = lib().tflows_ic_apply_device(self._h, ctypes.byref(opts) if opts else None,
+                                          _ptr(val), _ptr(r), _ptr(z), _stream(),
+                                          ctypes.byref(res))
+        if st != OK:
+            raise SolverError(st, last_error())
+        return res.as_dict()
+
     def spmv(self, val, x, y, repeat=1, fp32=False):
         sec = ctypes.c_double()
         st = lib().tflows_spmv_device(self._h, _ptr(val), _ptr(x), _ptr(y), int(repeat),

@@ -94,6 +94,62 @@ __device__ __forceinline__ void raise_abort(DevCtl* c, int status, int where) {
     atomicExch(&c->abort, 1);
 }
 
+// ---- shared-memory staging with bulk async copies --------------------------------
+// The tiled IC sweeps stream each wavefront step's record (contiguous in its
+// step-major layout) into a ring of shared-memory slots with the bulk copy
+// engine (cp.async.bulk, global -> shared), one mbarrier per slot: the
+// issuing thread announces the byte count (arrive.expect_tx), the copy
+// completes the transaction, and the consumers wait on the slot's phase
+// parity.  Sizes are multiples of 16 bytes and both addresses 16-byte
+// aligned (the host sizes the layout so).
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+// Makes the initialised barriers visible to the async proxy (the bulk copies).
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// `bytes` from global `src` into this CTA's shared `dst`, completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+// Orders this thread's earlier generic-proxy accesses before its later
+// async-proxy accesses: in shared memory (the block's reads of a ring slot
+// before the bulk copy that refills it; cheap, issued every step) or in
+// global memory (words written before a barrier that bulk copies read after
+// it; once per sweep or tile, as it waits for this thread's global accesses).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 // ---- value-as-flag cells ------------------------------------------------------
 template <typename T> struct Cell;
 template <> struct Cell<double> {

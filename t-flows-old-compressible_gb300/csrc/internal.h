@@ -39,6 +39,10 @@ struct DeviceTopology {
     int* perm_f = nullptr;
     int* perm_b = nullptr;
     int* tpos = nullptr;       // transpose map (lazy)
+    // box numbering (0 = not a box): row = x + nx (y + ny z), each row holding
+    // exactly its 7-point neighbours in ascending order (what TopolM builds
+    // for a structured block); enables the tiled IC sweeps
+    int box_nx = 0, box_ny = 0, box_nz = 0;
     // host copies (0-based) for lazy derived data
     std::vector<int> h_rowptr, h_col, h_diag;
 };
@@ -61,6 +65,10 @@ struct Workspace {
     void* ctl = nullptr;       // DevCtl
     void* state = nullptr;     // DevState
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // step records and cells of the tiled IC sweeps, per working precision
+    unsigned char* tile64 = nullptr;
+    unsigned char* tile32 = nullptr;
+    size_t tile_cap64 = 0, tile_cap32 = 0;  // bytes
 };
 constexpr int kVecs = 14;
 
@@ -86,6 +94,8 @@ struct SolveRequest {
     int sweep_mult = 0;     // IC sweep warps per chunk of the widest level (0 = 4)
     int sweep_gate = -1;    // IC sweeps: gated polling 1 / 0, -1 = process default
     int autotune = 0;       // take block/rows_per_warp/sweep_mult from the tuner
+    int ic_tiled = -1;      // exact IC on a box pattern: 1 tiled sweeps, 0 level
+                            // sweeps, -1 tiled unless TFLOWS_IC_TILED=0
 };
 
 struct SolveReport {
@@ -129,6 +139,10 @@ cudaError_t permute_transposed(const DeviceTopology& t, Workspace& ws, const dou
 // Runs a full solve. x (n) and r (n, holds b on entry) are device FP64 arrays.
 int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
               cudaStream_t s, SolveReport& rep);
+// The IC(0) pivots and one apply z = M^-1 r in FP64 (reference or contracted
+// arithmetic per rq.precision; tiled or level sweeps per rq.ic_tiled).
+int run_ic_apply(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, const double* r,
+                 double* z, cudaStream_t s, SolveReport& rep);
 // Prec1 only: D (n, device FP64).
 int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, double timeout_s,
               cudaStream_t s, SolveReport& rep);
@@ -148,6 +162,12 @@ cudaError_t run_resid(const DeviceTopology& t, Workspace& ws, const double* x, d
                       cudaStream_t s);
 // The grid a solve with this request would launch (co-residency included).
 int planned_grid(const DeviceTopology& t, const SolveRequest& rq);
+// Tiled IC sweeps: whether this request runs them, the dynamic shared memory
+// a launch needs for them, and their step records (allocated here, so call
+// before a stream capture).
+bool tiled_ic(const DeviceTopology& t, const SolveRequest& rq);
+unsigned tile_smem_for(const DeviceTopology& t, const SolveRequest& rq);
+cudaError_t ensure_tiles(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq);
 cudaError_t run_spmv(const DeviceTopology& t, Workspace& ws, const double* x, double* y, bool fp32,
                      int repeat, cudaStream_t s, float* ms);
 cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, const double* x,
@@ -159,8 +179,8 @@ int report_status(int status, const std::string& msg);
 // The persistent kernels, built twice: krylov.cu with the reference's
 // arithmetic (separate rounded products and sums, dividing diagonal) and
 // krylov_fma.cu with fused multiply-adds (TFLOWS_FP64_FMA and mixed solves).
-enum class KernelId { Cg, Cgs, BicgTrue, Prec1, MixedRestart, MixedReliable, MixedCgs, BatchFp64,
-                      BatchMixed };
+enum class KernelId { Cg, Cgs, BicgTrue, Prec1, IcApply, MixedRestart, MixedReliable, MixedCgs,
+                      BatchFp64, BatchMixed };
 const void* ref_kernel(KernelId id);
 const void* fma_kernel(KernelId id);
 

@@ -11,6 +11,9 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 namespace tflows {
 
@@ -56,6 +59,48 @@ __global__ void permute_kernel(int n, const int* __restrict__ rowptr,
             if (s64) s64[o] = a;
             if (s32) s32[o] = (float)a;
             if (s16) s16[o] = __bfloat16_as_ushort(__double2bfloat16(a));
+        }
+    }
+}
+
+// Coefficient fields of the tiled IC sweeps' step records from the SELL
+// values (the same numbers the level-ordered sweeps read: FP64, FP32, or
+// BF16 bit patterns).  For the row of thread t of tile k at step s, the
+// forward record (k, s) gets its lower coefficients by neighbour (z-1, y-1,
+// x-1) and the backward record its upper ones (x+1, y+1, z+1); absent
+// neighbours and idle slots hold 0.
+template <typename L>
+__global__ void tile_permute_kernel(int nx, int ny, int nz, int ty, int ntx, int steps,
+                                    long long total, const long long* __restrict__ soff,
+                                    const int* __restrict__ meta, const L* __restrict__ sval,
+                                    unsigned char* fwd, unsigned char* bwd, unsigned rec_f,
+                                    unsigned rec_b) {
+    const int B = kTileX * ty;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int t = (int)(i % B);
+        const long long ks = i / B;
+        const int s = (int)(ks % steps), k = (int)(ks / steps);
+        const int lx = t % kTileX, ly = t / kTileX;
+        const int x = (k % ntx) * kTileX + lx, y = (k / ntx) * ty + ly, z = s - lx - ly;
+        L a[6] = {L(0), L(0), L(0), L(0), L(0), L(0)};
+        if (x < nx && y < ny && z >= 0 && z < nz) {
+            const int row = x + nx * (y + ny * z);
+            const long long base = soff[row >> 5] + (row & 31);
+            int q = 0;
+            if (z > 0) a[0] = sval[base + 32LL * q++];
+            if (y > 0) a[1] = sval[base + 32LL * q++];
+            if (x > 0) a[2] = sval[base + 32LL * q++];
+            q = (meta[row] >> 16) + 1;  // first entry after the diagonal
+            if (x < nx - 1) a[3] = sval[base + 32LL * q++];
+            if (y < ny - 1) a[4] = sval[base + 32LL * q++];
+            if (z < nz - 1) a[5] = sval[base + 32LL * q++];
+        }
+        L* rf = reinterpret_cast<L*>(fwd + ks * rec_f);
+        L* rb = reinterpret_cast<L*>(bwd + ks * rec_b);
+        for (int f = 0; f < 3; ++f) {
+            rf[f * B + t] = a[f];
+            rb[f * B + t] = a[3 + f];
         }
     }
 }
@@ -226,7 +271,7 @@ cudaError_t ensure_workspace(Workspace& ws, const DeviceTopology& t) {
 void free_workspace(Workspace& ws) {
     for (void* p : {(void*)ws.sval64, (void*)ws.sval32, (void*)ws.vec64, (void*)ws.vec32,
                     (void*)ws.csr_val, (void*)ws.partials, ws.ctl, ws.state, (void*)ws.svalT64,
-                    (void*)ws.sval16})
+                    (void*)ws.sval16, (void*)ws.tile64, (void*)ws.tile32})
         if (p) cudaFree(p);
     if (ws.ev0) cudaEventDestroy(ws.ev0);
     if (ws.ev1) cudaEventDestroy(ws.ev1);
@@ -283,17 +328,33 @@ Vecs<T> carve(T* base, size_t cap, T* x, T* r) {
     return v;
 }
 
+// Lets a persistent kernel take the tiled sweeps' dynamic shared memory
+// (once per kernel; a launch without it is unaffected).
+void allow_dynamic_smem(const void* kernel, unsigned bytes) {
+    if (bytes <= 48u * 1024u) return;
+    static std::mutex mu;
+    static std::vector<std::pair<const void*, unsigned>> done;
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto& d : done)
+        if (d.first == kernel && d.second >= bytes) return;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
+        cudaSuccess)
+        done.emplace_back(kernel, bytes);
+}
+
 template <typename K>
-int max_coresident(K kernel, int block) {
+int max_coresident(K kernel, int block, unsigned smem = 0) {
+    allow_dynamic_smem((const void*)kernel, smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
     return std::max(1, per_sm) * sms();
 }
 
 template <typename K, typename P>
-cudaError_t launch_coop(K kernel, P& params, int grid, int block, cudaStream_t s) {
+cudaError_t launch_coop(K kernel, P& params, int grid, int block, cudaStream_t s,
+                        unsigned smem = 0) {
     void* args[] = {&params};
-    return cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(block), args, 0, s);
+    return cudaLaunchCooperativeKernel((const void*)kernel, dim3(grid), dim3(block), args, smem, s);
 }
 
 int block_of(const SolveRequest& rq) { return rq.block > 0 ? rq.block : kBlock; }
@@ -342,6 +403,125 @@ int run_prec1(const DeviceTopology& t, Workspace& ws, int prec, double* D, doubl
 
 namespace {
 
+// Exact IC(0) on a box-numbered pattern runs the tiled sweeps, unless the
+// request asks for the level-ordered ones or TFLOWS_IC_TILED=0 does.
+bool tiles_env_on() {
+    static const int v = [] {
+        const char* e = std::getenv("TFLOWS_IC_TILED");
+        return e && *e ? (std::atoi(e) != 0) : 1;
+    }();
+    return v;
+}
+
+size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+struct TileGeom {
+    int ty = 0, ntx = 0, nty = 0, steps = 0;
+    long long slots = 0;
+};
+
+TileGeom tile_geom(const DeviceTopology& t, int block) {
+    TileGeom g;
+    g.ty = block / kTileX;
+    g.ntx = (t.box_nx + kTileX - 1) / kTileX;
+    g.nty = (t.box_ny + g.ty - 1) / g.ty;
+    g.steps = kTileX + g.ty + t.box_nz - 2;
+    g.slots = (long long)g.ntx * g.nty * g.steps * block;
+    return g;
+}
+
+// Coefficient and value bytes of a request's records.
+void tile_elem(const SolveRequest& rq, unsigned& ls, unsigned& sv) {
+    if (rq.precision == 1) {
+        ls = rq.ic_bf16 ? 2u : 4u;
+        sv = 4u;
+    } else {
+        ls = 8u;
+        sv = 8u;
+    }
+}
+
+// Forward and backward records (three coefficient and at most three value
+// fields each) plus the two cell arrays.
+size_t tile_buffer_bytes(long long slots, unsigned ls, unsigned sv) {
+    return 2 * align256((size_t)slots * (3 * ls + 3 * sv)) + 2 * align256((size_t)slots * sv);
+}
+
+}  // namespace
+
+bool tiled_ic(const DeviceTopology& t, const SolveRequest& rq) {
+    if (rq.prec != 2 || rq.ic_sweeps > 0 || t.box_nx <= 0 || rq.ic_tiled == 0) return false;
+    if (rq.ic_tiled < 0 && !tiles_env_on()) return false;
+    const int B = rq.block > 0 ? rq.block : kBlock;
+    return B % 32 == 0 && B >= 64 && B <= kMaxBlock;
+}
+
+unsigned tile_smem_for(const DeviceTopology& t, const SolveRequest& rq) {
+    if (!tiled_ic(t, rq)) return 0;
+    unsigned ls, sv;
+    tile_elem(rq, ls, sv);
+    return tile_smem_bytes(rq.block > 0 ? rq.block : kBlock, ls, sv);
+}
+
+cudaError_t ensure_tiles(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq) {
+    if (!tiled_ic(t, rq)) return cudaSuccess;
+    const TileGeom tg = tile_geom(t, rq.block > 0 ? rq.block : kBlock);
+    const bool mixed = rq.precision == 1;
+    // the FP32 buffer is sized for FP32 coefficients, which covers BF16 ones
+    const size_t need = mixed ? tile_buffer_bytes(tg.slots, 4, 4) : tile_buffer_bytes(tg.slots, 8, 8);
+    unsigned char*& buf = mixed ? ws.tile32 : ws.tile64;
+    size_t& cap = mixed ? ws.tile_cap32 : ws.tile_cap64;
+    if (need <= cap) return cudaSuccess;
+    if (buf) cudaFree(buf);
+    buf = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&buf, need);
+    if (e == cudaSuccess) cap = need;
+    return e;
+}
+
+namespace {
+
+// The tiled-sweep descriptor of a solve and the coefficient fields of its
+// records, queued on stream s from the SELL values (`sval`: FP64, FP32 or
+// BF16 bits).
+template <typename T, typename L>
+cudaError_t fill_tiles(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq,
+                       const L* sval, Tiles<T>& tl, cudaStream_t s) {
+    std::memset(&tl, 0, sizeof(tl));
+    if (!tiled_ic(t, rq)) return cudaSuccess;
+    cudaError_t e = ensure_tiles(t, ws, rq);
+    if (e != cudaSuccess) return e;
+    const int B = rq.block > 0 ? rq.block : kBlock;
+    const TileGeom tg = tile_geom(t, B);
+    unsigned char* p = sizeof(T) == 8 ? ws.tile64 : ws.tile32;
+    // the contracted FP64 build multiplies by 1/(D+TINY) in the middle step
+    const int recip = sizeof(T) == 8 && rq.precision == 2 ? 1 : 0;
+    const unsigned ls = sizeof(L), sv = sizeof(T);
+    const size_t recs = align256((size_t)tg.slots * (3 * ls + 3 * sv));
+    tl.on = 1;
+    tl.nx = t.box_nx;
+    tl.ny = t.box_ny;
+    tl.nz = t.box_nz;
+    tl.ty = tg.ty;
+    tl.ntx = tg.ntx;
+    tl.nty = tg.nty;
+    tl.steps = tg.steps;
+    tl.lu_bf16 = sizeof(L) == 2 ? 1 : 0;
+    tl.recip = recip;
+    tl.rec_f = B * (3 * ls + (recip ? 3 : 2) * sv);
+    tl.rec_b = B * (3 * ls + 3 * sv);
+    tl.fwd = p;
+    tl.bwd = p + recs;
+    tl.wt = reinterpret_cast<T*>(p + 2 * recs);
+    tl.zt = reinterpret_cast<T*>(p + 2 * recs + align256((size_t)tg.slots * sv));
+    const int nb = (int)std::min<long long>(std::max<long long>(1, (tg.slots + 255) / 256), sms() * 16LL);
+    tile_permute_kernel<L><<<nb, 256, 0, s>>>(t.box_nx, t.box_ny, t.box_nz, tg.ty, tg.ntx, tg.steps,
+                                              tg.slots, t.soff, t.meta, sval, tl.fwd, tl.bwd,
+                                              tl.rec_f, tl.rec_b);
+    return cudaGetLastError();
+}
+
 // Parameters of one FP64 (reference arithmetic) solve; queues the control
 // block / counter resets and the IC sentinel fill on stream s.
 cudaError_t prepare_fp64(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x,
@@ -365,11 +545,13 @@ cudaError_t prepare_fp64(const DeviceTopology& t, Workspace& ws, const SolveRequ
     P.timeout_cyc = timeout_cycles(rq.timeout_s);
     P.mode = 0;
     P.stall = rq.inject_stall;
+    P.cfg.ic_sweeps = rq.prec == 2 ? std::max(rq.ic_sweeps, 0) : 0;
     cudaError_t e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
     if (rq.prec == 2) {
         const long long nvec = (long long)t.nslices * kWarp;
         fill_sentinel_kernel<double>
             <<<std::min(1024, (int)((nvec + 255) / 256)), 256, 0, s>>>(P.v.w, nvec);
+        if (e == cudaSuccess) e = fill_tiles<double, double>(t, ws, rq, ws.sval64, P.m.tile, s);
     }
     return e;
 }
@@ -408,6 +590,9 @@ cudaError_t prepare_mixed(const DeviceTopology& t, Workspace& ws, const SolveReq
         if (!ws.sval16) return cudaErrorInvalidValue;  // filled by permute_values
         P.m32.lu16 = ws.sval16;
     }
+    if (e == cudaSuccess && rq.prec == 2)
+        e = rq.ic_bf16 ? fill_tiles<float, unsigned short>(t, ws, rq, ws.sval16, P.m32.tile, s)
+                       : fill_tiles<float, float>(t, ws, rq, ws.sval32, P.m32.tile, s);
     P.ctl = (DevCtl*)ws.ctl;
     P.state = (DevState*)ws.state;
     P.partials = ws.partials;
@@ -430,9 +615,13 @@ double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevSta
     // the row metadata, D and the right-hand side read and the result written
     // per triangle.  Jacobi sweeps: each sweep reads one triangle's entries.
     const double offd = (double)std::max(0, t.nnz - t.n);
+    // The tiled sweeps read no indices: the factor entries once, and per row
+    // D twice, the right-hand side once, w written and read, z written.
+    const bool tiled = tiled_ic(t, rq);
     auto ic_bytes = [&](double sv, double sx) {
-        if (rq.precision == 1 && rq.ic_sweeps > 0)
+        if (rq.ic_sweeps > 0)
             return rq.ic_sweeps * (offd * (sv + 4.0) + 2.0 * t.n * (4.0 + 3.0 * sx));
+        if (tiled) return offd * sv + 6.0 * t.n * sx;
         return offd * (sv + 4.0) + 2.0 * t.n * (4.0 + 3.0 * sx);
     };
     if (rq.precision == 1) {
@@ -474,9 +663,10 @@ template <typename K, typename P>
 int launch_and_report(K kern, P& params, const DeviceTopology& t, Workspace& ws,
                       const SolveRequest& rq, cudaStream_t s, SolveReport& rep, cudaError_t e) {
     const int block = block_of(rq);
-    const int grid = choose_grid(t, rq, max_coresident(kern, block));
+    const unsigned smem = tile_smem_for(t, rq);
+    const int grid = choose_grid(t, rq, max_coresident(kern, block, smem));
     cudaEventRecord(ws.ev0, s);
-    if (e == cudaSuccess) e = launch_coop(kern, params, grid, block, s);
+    if (e == cudaSuccess) e = launch_coop(kern, params, grid, block, s, smem);
     rep.block = block;
     rep.grid = grid;
     cudaEventRecord(ws.ev1, s);
@@ -502,6 +692,7 @@ const void* ref_kernel(KernelId id) {
         case KernelId::Cgs: return (const void*)ref::krylov_kernel<double, 2>;
         case KernelId::BicgTrue: return (const void*)ref::krylov_kernel<double, 3>;
         case KernelId::Prec1: return (const void*)ref::krylov_kernel<double, 9>;
+        case KernelId::IcApply: return (const void*)ref::krylov_kernel<double, 8>;
         case KernelId::BatchFp64: return (const void*)ref::batch_kernel<0>;
         default: return nullptr;  // mixed solves are built with contraction only
     }
@@ -529,7 +720,30 @@ const void* batch_kernel_for(int precision) {
 }  // namespace
 
 int planned_grid(const DeviceTopology& t, const SolveRequest& rq) {
-    return choose_grid(t, rq, max_coresident(solver_kernel(rq), block_of(rq)));
+    return choose_grid(t, rq, max_coresident(solver_kernel(rq), block_of(rq), tile_smem_for(t, rq)));
+}
+
+int run_ic_apply(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq0, const double* r,
+                 double* z, cudaStream_t s, SolveReport& rep) {
+    SolveRequest rq = rq0;
+    rq.prec = 2;
+    rq.method = 0;
+    rq.precision = rq0.precision == 2 ? 2 : 0;
+    double* R = ws.vec64 + 12 * ws.vec_cap;
+    KParams<double> P;
+    cudaError_t e = cudaMemcpyAsync(R, r, sizeof(double) * t.n, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = prepare_fp64(t, ws, rq, ws.vec64 + 11 * ws.vec_cap, R, s, P);
+    const void* kern = rq.precision == 2 ? fma_kernel(KernelId::IcApply) : ref_kernel(KernelId::IcApply);
+    const int st = launch_and_report(kern, P, t, ws, rq, s, rep, e);
+    if (st == ST_CUDA_ERROR) return st;
+    e = cudaMemcpyAsync(z, P.v.z, sizeof(double) * t.n, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        rep.status = ST_CUDA_ERROR;
+        rep.message = cudaGetErrorString(e);
+    }
+    rep.bytes = 0.0;
+    return rep.status;
 }
 
 int run_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, double* x, double* r,
@@ -628,12 +842,15 @@ int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s)
         }
     const void* kern = batch_kernel_for(precision);
     const int block = block_of(specs[0].rq);
-    for (auto& sp : specs)
+    unsigned smem = 0;
+    for (auto& sp : specs) {
         if (block_of(sp.rq) != block) {
             fail_all(specs, ST_BAD_INPUT, "one block size per batched launch");
             return ST_BAD_INPUT;
         }
-    const int maxb = max_coresident(kern, block);
+        smem = std::max(smem, tile_smem_for(*sp.t, sp.rq));
+    }
+    const int maxb = max_coresident(kern, block, smem);
     if (count > maxb) {
         fail_all(specs, ST_BAD_INPUT,
                  "more systems than co-resident blocks (" + std::to_string(maxb) + ")");
@@ -695,6 +912,7 @@ int batch_enqueue(BatchLaunch* L, std::vector<BatchSpec>& specs, cudaStream_t s)
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(total);
         cfg.blockDim = dim3(block);
+        cfg.dynamicSmemBytes = smem;
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeCooperative;

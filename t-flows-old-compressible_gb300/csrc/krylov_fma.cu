@@ -19,6 +19,7 @@ const void* fma_kernel(KernelId id) {
         case KernelId::Cg: return (const void*)fma::krylov_kernel<double, 0>;
         case KernelId::Cgs: return (const void*)fma::krylov_kernel<double, 2>;
         case KernelId::BicgTrue: return (const void*)fma::krylov_kernel<double, 3>;
+        case KernelId::IcApply: return (const void*)fma::krylov_kernel<double, 8>;
         case KernelId::MixedRestart: return (const void*)fma::mixed_kernel<0>;
         case KernelId::MixedReliable: return (const void*)fma::mixed_kernel<1>;
         case KernelId::MixedCgs: return (const void*)fma::mixed_kernel<2>;

@@ -42,6 +42,49 @@ __device__ __forceinline__ T tiny_v() {
 // Reduction slots in the partials array (each slot = one value per block).
 enum : int { SLOT_A = 0, SLOT_B = 4, SLOT_C = 8, SLOT_D = 12, NUM_SLOTS = 16 };
 
+// Tiled IC(0) sweeps on a box-numbered pattern (row = x + nx (y + ny z),
+// 7-point stencil in TopolM order).  Each block owns tiles of 16 x ty
+// columns (ty = block size / 16) that run through all z; its threads walk
+// their columns along the wavefront step s = lx + ly + z.  Everything a step
+// reads sits in one contiguous record per (tile, step), fields of `block`
+// entries each, so one bulk copy stages it:
+//   forward record:  lower coefficients (z-1, y-1, x-1) | D | rhs | [1/(D+TINY)]
+//   backward record: upper coefficients (x+1, y+1, z+1) | D | mid | rhs
+// (mid = w / (D + TINY), written by the forward sweep; the reciprocal field
+// exists only where the forward sweep multiplies by it: the contracted FP64
+// build).  The cells of slot (k, s, t) = (k * steps + s) * block + t carry
+// the results a neighbouring tile reads.
+constexpr int kTileX = 16;     // tile width in x (columns per tile row)
+constexpr int kTileRing = 4;   // wavefront steps staged ahead in shared memory
+
+template <typename T>
+struct Tiles {
+    int on;                 // 1: IC applies of this solve run the tiled sweeps
+    int nx, ny, nz;         // box dimensions
+    int ty;                 // tile height in y (block size / 16)
+    int ntx, nty;           // tiles along x and y
+    int steps;              // wavefront steps per tile: 16 + ty + nz - 2
+    int lu_bf16;            // coefficients stored as BF16 bit patterns (FP32 solves)
+    int recip;              // forward: mid = w * (1/(D+TINY)) instead of w / (D+TINY)
+    unsigned rec_f, rec_b;  // bytes of one forward / backward record
+    unsigned char* fwd;     // [tile][step] forward records
+    unsigned char* bwd;     // [tile][step] backward records
+    T* wt;                  // forward results by slot (value-as-flag cells)
+    T* zt;                  // backward results by slot (value-as-flag cells)
+};
+
+// Bytes of one ring slot (the larger record: three coefficients and three
+// value fields), rounded to 128, and of the whole dynamic shared-memory block
+// of a tiled solve (barriers and flags, the ring, the neighbour exchange).
+__host__ __device__ constexpr unsigned tile_slot_bytes(unsigned block, unsigned coef_bytes,
+                                                       unsigned val_bytes) {
+    return (block * (3 * coef_bytes + 3 * val_bytes) + 127u) / 128u * 128u;
+}
+__host__ __device__ constexpr unsigned tile_smem_bytes(unsigned block, unsigned coef_bytes,
+                                                       unsigned val_bytes) {
+    return 128u + kTileRing * tile_slot_bytes(block, coef_bytes, val_bytes) + 2u * block * val_bytes;
+}
+
 template <typename T>
 struct Mat {
     int n;
@@ -68,6 +111,7 @@ struct Mat {
     int sweep_mult;  // sweep warps per chunk of the widest level (0 = default)
     int sweep_sleep; // longest pause between polls of a sweep cell, ns (0: none)
     int sweep_gate;  // 1: a waiting warp polls one representative cell first
+    Tiles<T> tile;   // tiled IC sweeps (tile.on = 0: level-ordered sweeps)
 };
 
 template <typename T>
@@ -481,7 +525,7 @@ __device__ bool prec1_phase(Grid& g, const Mat<T>& m, T* D, int prec) {
 // does: forward w_i = D_i (rhs_i - sum_{k<i} a_ik w_k); middle
 // w_i / (D_i + TINY); backward z_i = D_i (mid_i - sum_{k>i} a_ik z_k).
 // `w` cells must hold the sentinel on entry and hold it again on exit.
-// The backward phase calls `epi(row, z_row)` for fused per-row work.
+// The backward phase calls `epi(row, z_row, rhs_row)` for fused per-row work.
 template <typename T, typename Epi>
 __device__ bool ic_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* w, T* z, Epi epi) {
     bool ok = true;
@@ -520,7 +564,7 @@ __device__ bool ic_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* 
                             [&](T zi) {
                                 Cell<T>::store(z + row, zi);
                                 w[row] = Cell<T>::sentinel();
-                                epi(row, zi);
+                                epi(row, zi, rhs[row]);
                             });
     }
     return ok;
@@ -576,7 +620,7 @@ __device__ __forceinline__ void tri_jacobi(const Grid& g, const Mat<T>& m, const
 
 // k forward sweeps ping-pong between w and s (the last one stores the middle
 // vector), k backward sweeps between z and the other buffer, the last one
-// into z with `epi(row, z_row)` fused.  No barrier after the last sweep.
+// into z with `epi(row, z_row, rhs_row)` fused.  No barrier after the last sweep.
 template <typename T, typename Epi>
 __device__ bool ic_jacobi_apply(Grid& g, const Mat<T>& m, const T* D, const T* rhs, T* w, T* sb,
                                 T* z, int k, Epi epi) {
@@ -600,7 +644,7 @@ __device__ bool ic_jacobi_apply(Grid& g, const Mat<T>& m, const T* D, const T* r
             if (!grid_sync(g, 24)) return false;
         } else {
             tri_jacobi<false>(g, m, D, mid, y, o, [&](int i, T v) {
-                epi(i, v);
+                epi(i, v, rhs[i]);
                 return v;
             });
         }
@@ -608,14 +652,412 @@ __device__ bool ic_jacobi_apply(Grid& g, const Mat<T>& m, const T* D, const T* r
     return true;
 }
 
-// The IC(0) apply the solve was configured for: exact sync-free sweeps, or
-// `sweeps` Jacobi sweeps per triangle (FP32 inner solves only).
+// ---- tiled IC(0) sweeps (box-numbered patterns) --------------------------------
+// Forward: row (x, y, z) needs (x, y, z-1), (x, y-1, z), (x-1, y, z), in the
+// stored order of its lower entries (columns ascending, CG.f90:135-142).
+// Thread (lx, ly) of a tile walks its column: at step s it computes the row
+// with z = s - lx - ly.  Its z-1 input is its own result of step s-1, its
+// y-1 and x-1 inputs are the results of threads (lx, ly-1) and (lx-1, ly)
+// at step s-1, exchanged through shared memory with one block barrier per
+// step -- or, on the tile's low edges, the cells of the neighbouring tiles,
+// which run the same steps ahead of this one (tiles are taken in increasing
+// index, each depending only on lower ones, all blocks resident, so the
+// sweep cannot deadlock).  Backward mirrors it (x+1, y+1, z+1; tiles and
+// steps in decreasing order).  Each row combines the same operands in the
+// same order as the sequential sweep (CG.f90:135-156), so in the
+// reference-arithmetic build the result is bit-identical to it and to the
+// level-ordered sweeps.
+//
+// Each step's record is staged into a ring of kTileRing shared-memory slots
+// by one bulk async copy issued kTileRing steps ahead (one elected thread,
+// one mbarrier per slot).  The right-hand side enters the forward records
+// through a gather each block runs for its own tiles before their first
+// step; the neighbour tiles' edge cells are loaded two steps ahead and
+// polled again only if they were not ready yet.
+
+constexpr int kTileCellAhead = 2;  // steps ahead for the neighbour edge cells
+
+struct TileSmem {
+    unsigned long long* bar;  // kTileRing barriers
+    volatile int* fail;       // set by a thread whose wait gave up
+    int* phase;               // ring slots' phase parities between sweeps
+    unsigned char* ring;
+    unsigned slot;            // bytes per ring slot
+};
+
+template <typename T>
+__device__ __forceinline__ TileSmem tile_smem(const Tiles<T>& tl) {
+    extern __shared__ __align__(128) unsigned char tf_smem[];
+    TileSmem m;
+    m.bar = reinterpret_cast<unsigned long long*>(tf_smem);
+    m.fail = reinterpret_cast<volatile int*>(tf_smem + 64);
+    m.phase = reinterpret_cast<int*>(tf_smem + 68);
+    m.ring = tf_smem + 128;
+    m.slot = tile_slot_bytes(blockDim.x, tl.lu_bf16 ? 2u : (unsigned)sizeof(T), (unsigned)sizeof(T));
+    return m;
+}
+
+// Byte offset of value field v (0 = D, 1 = rhs / mid, 2 = 1/(D+TINY) / rhs)
+// in a record, after the three coefficient fields.
+template <typename T>
+__device__ __forceinline__ unsigned tile_vfield(const Tiles<T>& tl, int v) {
+    return blockDim.x * (3u * (tl.lu_bf16 ? 2u : (unsigned)sizeof(T)) + v * (unsigned)sizeof(T));
+}
+
+// Coefficient f of thread t in a staged record.
+template <typename T>
+__device__ __forceinline__ T tile_coef(const Tiles<T>& tl, const unsigned char* rec, int f, int t) {
+    if constexpr (sizeof(T) == 4) {
+        if (tl.lu_bf16) {
+            const unsigned short u =
+                reinterpret_cast<const unsigned short*>(rec + (size_t)f * blockDim.x * 2)[t];
+            return __uint_as_float((unsigned)u << 16);
+        }
+    }
+    return reinterpret_cast<const T*>(rec + (size_t)f * blockDim.x * sizeof(T))[t];
+}
+
+template <typename T>
+__device__ __forceinline__ T& tile_val(const Tiles<T>& tl, unsigned char* rec, int v, int t) {
+    return reinterpret_cast<T*>(rec + tile_vfield(tl, v))[t];
+}
+
+// One record into a ring slot, completing on the slot's barrier.
+__device__ __forceinline__ void tile_issue(unsigned char* slot, unsigned long long* bar,
+                                           const unsigned char* rec, unsigned bytes) {
+    mbar_expect_tx(bar, bytes);
+    bulk_g2s(slot, rec, bytes, bar);
+}
+
+// A prefetched neighbour cell, polled again (bounded) while it still holds
+// the sentinel.  On giving up: abort raised, the block's fail flag set.
+template <typename T>
+__device__ __forceinline__ T tile_cell(const Grid& g, const TileSmem& sm, const T* p, T v, int where) {
+    using C = Cell<T>;
+    if (C::bits(v) != C::kSentinel) return v;
+    const long long t0 = clock64();
+    unsigned spins = 0;
+    while (true) {
+        const auto b = C::load(p);
+        if (b != C::kSentinel) return C::value(b);
+        if ((++spins & 63u) == 0u) {
+            const bool quit = ld_relaxed_s32(&g.ctl->abort) != 0;
+            if (quit || clock64() - t0 > g.timeout_cyc) {
+                if (!quit) raise_abort(g.ctl, ST_TIMEOUT, where);
+                *sm.fail = 1;
+                return T(0);
+            }
+        }
+    }
+}
+
+// Waits for a ring slot's copy (bounded).  False: abort raised, fail set.
+__device__ __forceinline__ bool tile_wait(const Grid& g, const TileSmem& sm, int u, unsigned parity,
+                                          int where) {
+    if (mbar_try_wait(sm.bar + u, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(sm.bar + u, parity)) {
+        if (clock64() - t0 > g.timeout_cyc) {
+            raise_abort(g.ctl, ST_TIMEOUT, where);
+            *sm.fail = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+// After a failure at step index j: thread 0 waits (bounded) for the copies
+// still in flight into the ring (steps j+1 .. j+kTileRing-1 of this tile).
+__device__ __forceinline__ void tile_drain(const Grid& g, const TileSmem& sm, int j, int S,
+                                           unsigned phase) {
+    if (threadIdx.x != 0) return;
+    for (int jj = j + 1; jj < S && jj < j + kTileRing; ++jj) {
+        const int u = jj % kTileRing;
+        const long long t0 = clock64();
+        while (!mbar_try_wait(sm.bar + u, (phase >> u) & 1u))
+            if (clock64() - t0 > g.timeout_cyc) break;
+    }
+}
+
+// Once per solve, before the first apply (a grid barrier must follow): the
+// pivots (and the reciprocals) into both record kinds, sentinels into both
+// cell arrays, the ring barriers initialised.
+template <typename T>
+__device__ void tiles_init(Grid& g, const Mat<T>& m, const T* __restrict__ D) {
+    const Tiles<T>& tl = m.tile;
+    const int B = blockDim.x;
+    const long long total = (long long)tl.ntx * tl.nty * tl.steps * B;
+    const T sen = Cell<T>::sentinel();
+    for (long long i = g.tid; i < total; i += g.nt) {
+        const int t = (int)(i % B);
+        const long long ks = i / B;
+        const int s = (int)(ks % tl.steps), k = (int)(ks / tl.steps);
+        const int lx = t % kTileX, ly = t / kTileX;
+        const int x = (k % tl.ntx) * kTileX + lx, y = (k / tl.ntx) * tl.ty + ly, z = s - lx - ly;
+        const bool act = x < tl.nx && y < tl.ny && z >= 0 && z < tl.nz;
+        const T d = act ? D[x + tl.nx * (y + tl.ny * z)] : T(0);
+        unsigned char* rf = tl.fwd + ks * tl.rec_f;
+        unsigned char* rb = tl.bwd + ks * tl.rec_b;
+        tile_val(tl, rf, 0, t) = d;
+        tile_val(tl, rb, 0, t) = d;
+        if (tl.recip) tile_val(tl, rf, 2, t) = act ? T(1) / (d + tiny_v<T>()) : T(0);
+        tl.wt[i] = sen;
+        tl.zt[i] = sen;
+    }
+    const TileSmem sm = tile_smem(tl);
+    if (threadIdx.x == 0) {
+        for (int u = 0; u < kTileRing; ++u) mbar_init(sm.bar + u, 1);
+        *sm.fail = 0;
+        *sm.phase = 0;
+        mbar_init_fence();
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs) {
+    const Tiles<T>& tl = m.tile;
+    const TileSmem sm = tile_smem(tl);
+    const int B = blockDim.x, t = threadIdx.x, lx = t % kTileX, ly = t / kTileX;
+    const int S = tl.steps, ntiles = tl.ntx * tl.nty;
+    const size_t plane = (size_t)S * B;
+    T* nbv = reinterpret_cast<T*>(sm.ring + kTileRing * sm.slot);
+    const unsigned vf0 = tile_vfield(tl, 0), vf1 = tile_vfield(tl, 1), vf2 = tile_vfield(tl, 2);
+    __syncthreads();
+    unsigned phase = (unsigned)*sm.phase;
+    bool ok = true;
+    for (int k = g.bid; k < ntiles && ok; k += g.nblocks) {
+        const int x = (k % tl.ntx) * kTileX + lx, y = (k / tl.ntx) * tl.ty + ly;
+        const bool inb = x < tl.nx && y < tl.ny;
+        const size_t base = (size_t)k * plane;
+        unsigned char* recf = tl.fwd + (size_t)k * S * tl.rec_f;
+        unsigned char* recb = tl.bwd + (size_t)k * S * tl.rec_b;
+        // gather this tile's right-hand side into its forward records
+        // (eight independent loads in flight per thread)
+        for (int s0 = 0; s0 < S; s0 += 8) {
+            T v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int z = s0 + q - lx - ly;
+                v[q] = inb && z >= 0 && z < tl.nz && s0 + q < S ? rhs[x + tl.nx * (y + tl.ny * z)]
+                                                                : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (s0 + q < S) reinterpret_cast<T*>(recf + (size_t)(s0 + q) * tl.rec_f + vf1)[t] = v[q];
+        }
+        __syncthreads();
+        // edge cells of the left (x-1) and lower (y-1) tiles at step s
+        // (used only where that tile exists: x > 0 resp. y > 0)
+        const long long sb = (long long)base, sp = (long long)plane;
+        const T* xcell = tl.wt + (sb - sp + (long long)(kTileX - 1) * B + ly * kTileX + (kTileX - 1));
+        const T* ycell =
+            tl.wt + (sb - tl.ntx * sp + (long long)(tl.ty - 1) * B + (tl.ty - 1) * kTileX + lx);
+        if (t == 0) {
+            // the gathered words (and the records written before the sweep)
+            // and the previous tile's reads of the ring before the bulk copies
+            fence_proxy_async_global();
+            fence_proxy_async_smem();
+            for (int u = 0; u < kTileRing && u < S; ++u)
+                tile_issue(sm.ring + u * sm.slot, sm.bar + u, recf + (size_t)u * tl.rec_f, tl.rec_f);
+        }
+        T xpre[kTileCellAhead], ypre[kTileCellAhead];
+        auto prefetch = [&](int s, T& xp, T& yp) {
+            const int z = s - lx - ly;
+            if (inb && z >= 0 && z < tl.nz) {
+                if (lx == 0 && x > 0) xp = Cell<T>::value(Cell<T>::load(xcell + (size_t)s * B));
+                if (ly == 0 && y > 0) yp = Cell<T>::value(Cell<T>::load(ycell + (size_t)s * B));
+            }
+        };
+#pragma unroll
+        for (int u = 0; u < kTileCellAhead; ++u) {
+            xpre[u] = ypre[u] = T(0);
+            prefetch(u, xpre[u], ypre[u]);
+        }
+        T ycur = T(0);
+        for (int s0 = 0; s0 < S && ok; s0 += kTileRing) {
+#pragma unroll
+            for (int u = 0; u < kTileRing; ++u) {
+                const int s = s0 + u;
+                if (s >= S || !ok) break;
+                const int cu = u % kTileCellAhead;
+                tile_wait(g, sm, u, (phase >> u) & 1u, 26);
+                phase ^= 1u << u;
+                const int z = s - lx - ly;
+                if (inb && z >= 0 && z < tl.nz) {
+                    unsigned char* sl = sm.ring + u * sm.slot;
+                    const T ri = reinterpret_cast<const T*>(sl + vf1)[t];
+                    T acc = ri;
+                    if (z > 0) acc = acc - tile_coef(tl, sl, 0, t) * ycur;
+                    if (y > 0) {
+                        const T v = ly > 0 ? nbv[((s - 1) & 1) * B + t - kTileX]
+                                           : tile_cell(g, sm, ycell + (size_t)s * B, ypre[cu], 27);
+                        acc = acc - tile_coef(tl, sl, 1, t) * v;
+                    }
+                    if (x > 0) {
+                        const T v = lx > 0 ? nbv[((s - 1) & 1) * B + t - 1]
+                                           : tile_cell(g, sm, xcell + (size_t)s * B, xpre[cu], 27);
+                        acc = acc - tile_coef(tl, sl, 2, t) * v;
+                    }
+                    const T d = reinterpret_cast<const T*>(sl + vf0)[t];
+                    const T yv = acc * d;
+                    nbv[(s & 1) * B + t] = yv;
+                    ycur = yv;
+                    const size_t idx = base + (size_t)s * B + t;
+                    Cell<T>::store(tl.wt + idx, yv);
+                    // the middle step of CG.f90:144-146, for the backward sweep
+                    const T mid = tl.recip ? yv * reinterpret_cast<const T*>(sl + vf2)[t]
+                                           : yv / (d + tiny_v<T>());
+                    unsigned char* rb = recb + (size_t)s * tl.rec_b;
+                    reinterpret_cast<T*>(rb + vf1)[t] = mid;
+                    reinterpret_cast<T*>(rb + vf2)[t] = ri;
+                    tl.zt[idx] = Cell<T>::sentinel();
+                }
+                __syncthreads();
+                if (*sm.fail) {
+                    tile_drain(g, sm, s, S, phase);
+                    ok = false;
+                    break;
+                }
+                if (t == 0 && s + kTileRing < S) {
+                    fence_proxy_async_smem();  // the slot's reads before its refill
+                    tile_issue(sm.ring + u * sm.slot, sm.bar + u,
+                               recf + (size_t)(s + kTileRing) * tl.rec_f, tl.rec_f);
+                }
+                if (s + kTileCellAhead < S) prefetch(s + kTileCellAhead, xpre[cu], ypre[cu]);
+            }
+        }
+    }
+    __syncthreads();
+    if (t == 0) *sm.phase = (int)phase;
+    __syncthreads();
+    return ok;
+}
+
+template <typename T, typename Epi>
+__device__ bool tile_backward(Grid& g, const Mat<T>& m, T* __restrict__ zout, Epi epi) {
+    const Tiles<T>& tl = m.tile;
+    const TileSmem sm = tile_smem(tl);
+    const int B = blockDim.x, t = threadIdx.x, lx = t % kTileX, ly = t / kTileX;
+    const int S = tl.steps, ntiles = tl.ntx * tl.nty;
+    const size_t plane = (size_t)S * B;
+    T* nbv = reinterpret_cast<T*>(sm.ring + kTileRing * sm.slot);
+    const unsigned vf0 = tile_vfield(tl, 0), vf1 = tile_vfield(tl, 1), vf2 = tile_vfield(tl, 2);
+    __syncthreads();
+    unsigned phase = (unsigned)*sm.phase;
+    if (t == 0) fence_proxy_async_global();  // the records written before the barrier
+    bool ok = true;
+    // this block's tiles (g.bid, g.bid + nblocks, ...) in decreasing order
+    const int mine = g.bid < ntiles ? (ntiles - 1 - g.bid) / g.nblocks + 1 : 0;
+    for (int q = mine - 1; q >= 0 && ok; --q) {
+        const int k = g.bid + q * g.nblocks;
+        const int x = (k % tl.ntx) * kTileX + lx, y = (k / tl.ntx) * tl.ty + ly;
+        const bool inb = x < tl.nx && y < tl.ny;
+        const size_t base = (size_t)k * plane;
+        const unsigned char* recb = tl.bwd + (size_t)k * S * tl.rec_b;
+        // edge cells of the right (x+1) and upper (y+1) tiles at step s
+        // (used only where that tile exists: x < nx-1 resp. y < ny-1)
+        const long long sb = (long long)base, sp = (long long)plane;
+        const T* xcell = tl.zt + (sb + sp + ly * kTileX - (long long)(kTileX - 1) * B);
+        const T* ycell = tl.zt + (sb + tl.ntx * sp + lx - (long long)(tl.ty - 1) * B);
+        if (t == 0) {
+            fence_proxy_async_smem();
+            for (int u = 0; u < kTileRing && u < S; ++u)
+                tile_issue(sm.ring + u * sm.slot, sm.bar + u, recb + (size_t)(S - 1 - u) * tl.rec_b,
+                           tl.rec_b);
+        }
+        T xpre[kTileCellAhead], ypre[kTileCellAhead];
+        auto prefetch = [&](int s, T& xp, T& yp) {
+            const int z = s - lx - ly;
+            if (inb && z >= 0 && z < tl.nz) {
+                if (lx == kTileX - 1 && x < tl.nx - 1)
+                    xp = Cell<T>::value(Cell<T>::load(xcell + (size_t)s * B));
+                if (ly == tl.ty - 1 && y < tl.ny - 1)
+                    yp = Cell<T>::value(Cell<T>::load(ycell + (size_t)s * B));
+            }
+        };
+#pragma unroll
+        for (int u = 0; u < kTileCellAhead; ++u) {
+            xpre[u] = ypre[u] = T(0);
+            prefetch(S - 1 - u, xpre[u], ypre[u]);
+        }
+        T zcur = T(0);
+        for (int j0 = 0; j0 < S && ok; j0 += kTileRing) {
+#pragma unroll
+            for (int u = 0; u < kTileRing; ++u) {
+                const int j = j0 + u;
+                if (j >= S || !ok) break;
+                const int cu = u % kTileCellAhead;
+                const int s = S - 1 - j;
+                tile_wait(g, sm, u, (phase >> u) & 1u, 28);
+                phase ^= 1u << u;
+                const int z = s - lx - ly;
+                if (inb && z >= 0 && z < tl.nz) {
+                    const unsigned char* sl = sm.ring + u * sm.slot;
+                    const T d = reinterpret_cast<const T*>(sl + vf0)[t];
+                    T acc = reinterpret_cast<const T*>(sl + vf1)[t];  // mid
+                    const T ri = reinterpret_cast<const T*>(sl + vf2)[t];
+                    if (x < tl.nx - 1) {
+                        const T v = lx < kTileX - 1
+                                        ? nbv[((j - 1) & 1) * B + t + 1]
+                                        : tile_cell(g, sm, xcell + (size_t)s * B, xpre[cu], 29);
+                        acc = acc - tile_coef(tl, sl, 0, t) * v;
+                    }
+                    if (y < tl.ny - 1) {
+                        const T v = ly < tl.ty - 1
+                                        ? nbv[((j - 1) & 1) * B + t + kTileX]
+                                        : tile_cell(g, sm, ycell + (size_t)s * B, ypre[cu], 29);
+                        acc = acc - tile_coef(tl, sl, 1, t) * v;
+                    }
+                    if (z < tl.nz - 1) acc = acc - tile_coef(tl, sl, 2, t) * zcur;
+                    const T zi = acc * d;
+                    nbv[(j & 1) * B + t] = zi;
+                    zcur = zi;
+                    const size_t idx = base + (size_t)s * B + t;
+                    Cell<T>::store(tl.zt + idx, zi);
+                    tl.wt[idx] = Cell<T>::sentinel();
+                    const int row = x + tl.nx * (y + tl.ny * z);
+                    zout[row] = zi;
+                    epi(row, zi, ri);
+                }
+                __syncthreads();
+                if (*sm.fail) {
+                    tile_drain(g, sm, j, S, phase);
+                    ok = false;
+                    break;
+                }
+                if (t == 0 && j + kTileRing < S) {
+                    fence_proxy_async_smem();
+                    tile_issue(sm.ring + u * sm.slot, sm.bar + u,
+                               recb + (size_t)(s - kTileRing) * tl.rec_b, tl.rec_b);
+                }
+                if (j + kTileCellAhead < S) prefetch(s - kTileCellAhead, xpre[cu], ypre[cu]);
+            }
+        }
+    }
+    __syncthreads();
+    if (t == 0) *sm.phase = (int)phase;
+    __syncthreads();
+    return ok;
+}
+
+// z = IC(0) apply of rhs by the tiled sweeps; epi(row, z_row, rhs_row) per row.
+template <typename T, typename Epi>
+__device__ bool ic_tiled_apply(Grid& g, const Mat<T>& m, const T* rhs, T* z, Epi epi) {
+    const bool ok = tile_forward(g, m, rhs);
+    if (!grid_sync(g, 25) || !ok) return false;
+    return tile_backward(g, m, z, epi);
+}
+
+// The IC(0) apply the solve was configured for: `sweeps` Jacobi sweeps per
+// triangle (FP32 inner solves and contracted FP64 solves), else the exact
+// apply -- tiled sweeps on a box-numbered pattern, level-ordered sync-free
+// sweeps otherwise.  epi(row, z_row, rhs_row) runs once per row.
 template <typename T, typename Epi>
 __device__ __forceinline__ bool ic_precond(Grid& g, const Mat<T>& m, Vecs<T>& v, int sweeps,
                                            const T* rhs, T* z, Epi epi) {
-    if constexpr (sizeof(T) == 4) {
-        if (sweeps > 0) return ic_jacobi_apply(g, m, v.D, rhs, v.w, v.s, z, sweeps, epi);
-    }
+    if (sweeps > 0) return ic_jacobi_apply(g, m, v.D, rhs, v.w, v.s, z, sweeps, epi);
+    if (m.tile.on) return ic_tiled_apply(g, m, rhs, z, epi);
     return ic_apply(g, m, v.D, rhs, v.w, z, epi);
 }
 
@@ -633,6 +1075,9 @@ __device__ bool prologue(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         out.exit_kind = EXIT_ABORT;
         return false;
     }
+    // (IC pivots complete: prec1_phase ends with a barrier; the barrier
+    // below orders the tiled layout before the first apply)
+    if (cfg.do_prec1 && cfg.prec == 2 && m.tile.on) tiles_init(g, m, v.D);
     T acc[1] = {T(0)};
     TF_FOR4(g, m, i) {
         const V4<T> r = ld4(v.r + i);
@@ -701,9 +1146,8 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
     for (; iter <= cfg.maxiter; ++iter) {
         if (prec == 2) {
             T a[1] = {T(0)};
-            const T* rr = v.r;
-            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.r, v.z, [&](int row, T zi) {
-                a[0] += rr[row] * zi;
+            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.r, v.z, [&](int, T zi, T ri) {
+                a[0] += ri * zi;
             });
             publish_t<1>(g, SLOT_A, a);
             if (!grid_sync(g, 41) || !ok) { out.exit_kind = EXIT_ABORT; return; }
@@ -878,7 +1322,7 @@ __device__ void cgs_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& 
         }
         if (!grid_sync(g, 51)) { out.exit_kind = EXIT_ABORT; return; }
         if (prec == 2) {
-            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.u2, v.p2, [](int, T) {});
+            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.u2, v.p2, [](int, T, T) {});
             if (!grid_sync(g, 53) || !ok) { out.exit_kind = EXIT_ABORT; return; }
         }
         // v2 = A p2; alfa = rho / (r2, v2)
@@ -924,7 +1368,7 @@ __device__ void cgs_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& 
         if (!grid_sync(g, 55)) { out.exit_kind = EXIT_ABORT; return; }
         if (prec == 2) {
             T* xx = v.x;
-            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.t, v.p, [&](int row, T p1) {
+            const bool ok = ic_precond(g, m, v, cfg.ic_sweeps, v.t, v.p, [&](int row, T p1, T) {
                 xx[row] = xx[row] + alfa * p1;
             });
             if (!grid_sync(g, 57) || !ok) { out.exit_kind = EXIT_ABORT; return; }
@@ -1166,6 +1610,8 @@ static __device__ void mixed_solve(Grid& g, const Mat<double>& m64, const Mat<fl
     }
     publish<1>(g, SLOT_A, acc);
     if (!grid_sync(g, 71)) return;
+    // (the residual pass below ends with a barrier before the first apply)
+    if (c.prec == 2 && m32.tile.on) tiles_init(g, m32, v32.D);
     double tot[1];
     totals<1>(g, SLOT_A, tot);
     const double bnrm2 = sqrt(tot[0]);
@@ -1290,6 +1736,7 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
     }
     publish<1>(g, SLOT_A, acc);
     if (!grid_sync(g, 81)) return;
+    if (c.prec == 2 && m32.tile.on) tiles_init(g, m32, v.D);
     double tot[1];
     totals<1>(g, SLOT_A, tot);
     const double bnrm2 = sqrt(tot[0]);
@@ -1333,9 +1780,8 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
     };
     auto ic = [&](double& rz) -> bool {
         float a[1] = {0.f};
-        const float* rr = v.r;
-        const bool ok = ic_precond(g, m32, v, c.ic_sweeps, v.r, v.z, [&](int row, float zi) {
-            a[0] += rr[row] * zi;
+        const bool ok = ic_precond(g, m32, v, c.ic_sweeps, v.r, v.z, [&](int, float zi, float ri) {
+            a[0] += ri * zi;
         });
         publish_t<1>(g, SLOT_A, a);
         if (!grid_sync(g, 83) || !ok) return false;

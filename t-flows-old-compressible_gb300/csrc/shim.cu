@@ -81,6 +81,7 @@ void default_opts(tflows_options* o) {
     o->rows_per_warp = 0;
     o->sweep_warps = 0;
     o->sweep_gate = -1;
+    o->ic_tiled = -1;
     o->device = -1;
 }
 
@@ -197,8 +198,46 @@ cudaError_t build_patterns(DeviceTopology& t) {
     return cudaSuccess;
 }
 
+// Box numbering: row 0 holds columns 0, 1, nx, nx*ny; then every row i,
+// with x = i mod nx, y = (i / nx) mod ny, z = i / (nx ny), must hold exactly
+// its existing neighbours i-nx*ny, i-nx, i-1, i, i+1, i+nx, i+nx*ny in that
+// (ascending) order.  Boxes thinner than 2 cells in any direction are left
+// to the level-ordered sweeps.
+void detect_box(DeviceTopology& t) {
+    t.box_nx = t.box_ny = t.box_nz = 0;
+    const int n = t.n;
+    if (n < 8 || t.h_rowptr[1] - t.h_rowptr[0] != 4) return;
+    const int* c0 = t.h_col.data();
+    if (c0[0] != 0 || c0[1] != 1) return;
+    const long long nx = c0[2], nxy = c0[3];
+    if (nx < 2 || nxy <= nx || nxy % nx != 0 || n % nxy != 0) return;
+    const long long ny = nxy / nx, nz = n / nxy;
+    if (ny < 2 || nz < 2) return;
+    for (long long i = 0; i < n; ++i) {
+        const long long x = i % nx, y = (i / nx) % ny, z = i / nxy;
+        long long want[7];
+        int k = 0, dia = 0;
+        if (z > 0) want[k++] = i - nxy;
+        if (y > 0) want[k++] = i - nx;
+        if (x > 0) want[k++] = i - 1;
+        dia = k;
+        want[k++] = i;
+        if (x < nx - 1) want[k++] = i + 1;
+        if (y < ny - 1) want[k++] = i + nx;
+        if (z < nz - 1) want[k++] = i + nxy;
+        const int b = t.h_rowptr[i], e = t.h_rowptr[i + 1];
+        if (e - b != k || t.h_diag[i] - b != dia) return;
+        for (int j = 0; j < k; ++j)
+            if (t.h_col[b + j] != want[j]) return;
+    }
+    t.box_nx = (int)nx;
+    t.box_ny = (int)ny;
+    t.box_nz = (int)nz;
+}
+
 // SELL-32 layout: slice s holds rows 32s..32s+31, width = longest row.
 cudaError_t build_device(DeviceTopology& t) {
+    detect_box(t);
     const int n = t.n;
     t.nslices = (n + 31) / 32;
     std::vector<long long> soff((size_t)t.nslices + 1, 0);
@@ -424,11 +463,14 @@ SolveRequest make_request(const tflows_options& o, int method, int prec, int max
     rq.inner_rtol = o.inner_rtol;
     rq.inner_maxiter = o.inner_maxiter;
     rq.max_refinements = o.max_refinements;
-    // Jacobi sweeps and BF16 factor values exist only in the FP32 inner
-    // solves of the mixed mode with IC(0).
+    // BF16 factor values exist only in the FP32 inner solves of the mixed
+    // mode with IC(0); Jacobi sweeps there and in the contracted FP64 build
+    // (the reference-arithmetic build keeps the reference's exact apply).
     const bool mixed_ic = o.precision == TFLOWS_MIXED && prec == 2;
-    rq.ic_sweeps = mixed_ic ? std::max(o.ic_sweeps, 0) : 0;
+    const bool fma_ic = o.precision == TFLOWS_FP64_FMA && prec == 2;
+    rq.ic_sweeps = mixed_ic || fma_ic ? std::max(o.ic_sweeps, 0) : 0;
     rq.ic_bf16 = mixed_ic && o.ic_bf16 ? 1 : 0;
+    rq.ic_tiled = o.ic_tiled < 0 ? -1 : (o.ic_tiled != 0);
     rq.refine_restart = o.refine_restart;
     rq.inject_stall = o.inject_stall;
     rq.timeout_s = o.timeout_s > 0 ? o.timeout_s : 5.0;
@@ -1036,6 +1078,11 @@ int tflows_plan_create(tflows_plan** out, int count, tflows_topology* const* top
         plan->tuned = true;
         for (auto& r : plan->reps) r = SolveReport();
     }
+    // records of the tiled IC sweeps for the final launch shape (no
+    // allocation may happen inside the capture)
+    for (int k = 0; k < count && e == cudaSuccess; ++k)
+        e = ensure_tiles(*plan->specs[k].t, *plan->specs[k].ws, plan->specs[k].rq);
+    if (e != cudaSuccess) return cuda_fail(e, "tile buffers");
     plan->launch = batch_create();
     if ((e = batch_reserve(plan->launch, count, plan->specs[0].rq.block)) != cudaSuccess) {
         tflows_plan_destroy(plan.release());
@@ -1164,6 +1211,33 @@ int tflows_pattern_outer(tflows_topology* topo, const double* lambda, const doub
     cudaError_t e = run_pattern_outer(topo->t, lambda, x, grad_val, (cudaStream_t)stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_fail(e, "pattern outer");
+    t_status = TFLOWS_OK;
+    return TFLOWS_OK;
+}
+
+int tflows_ic_apply_device(tflows_topology* topo, const tflows_options* opt, const double* val,
+                           const double* r, double* z, void* stream, tflows_result* res) {
+    t_error.clear();
+    if (!topo || !val || !r || !z) return fail(TFLOWS_BAD_INPUT, "null argument");
+    std::lock_guard<std::mutex> lk(topo->mu);
+    cudaSetDevice(topo->t.device);
+    tflows_options o;
+    if (opt) o = *opt;
+    else default_opts(&o);
+    if (o.precision == TFLOWS_MIXED) return fail(TFLOWS_UNSUPPORTED, "the apply runs in FP64");
+    if (!topo->t.ic_ok)
+        return fail(TFLOWS_BAD_INPUT, "IC(0) needs a triangular-ordered pattern");
+    SolveRequest rq = make_request(o, TFLOWS_METHOD_CG, 2, 0, 0.0);
+    if (std::string msg; !shape_ok(rq, msg)) return fail(TFLOWS_BAD_INPUT, msg);
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = build_levels(topo->t);
+    if (e == cudaSuccess) e = ensure_workspace(topo->ws, topo->t);
+    if (e == cudaSuccess) e = permute_values(topo->t, topo->ws, val, true, false, s);
+    if (e != cudaSuccess) return cuda_fail(e, "ic apply");
+    SolveReport rep;
+    const int st = run_ic_apply(topo->t, topo->ws, rq, r, z, s, rep);
+    record(rep, res);
+    if (st != TFLOWS_OK) return fail(st, rep.message);
     t_status = TFLOWS_OK;
     return TFLOWS_OK;
 }

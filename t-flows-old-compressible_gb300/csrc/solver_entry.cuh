@@ -82,7 +82,8 @@ __device__ int status_of(const SolveOut& o, const DevCtl* ctl) {
     }
 }
 
-// METHOD: 0 CG (and BiCG), 2 CGS, 9 Prec1 only.
+// METHOD: 0 CG (and BiCG), 2 CGS, 3 true BiCG, 9 Prec1 only, 8 the IC(0)
+// pivots (Prec1 prec 2) and one apply z = M^-1 r (v.r in, v.z out).
 template <typename T, int METHOD>
 __global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax) krylov_kernel(KParams<T> P) {
     Grid g;
@@ -96,6 +97,14 @@ __global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax) krylov_kernel(KPar
     out.bnrm2 = 0.0;
     if (METHOD == 9) {
         bool ok = prec1_phase(g, P.m, P.v.D, P.cfg.prec);
+        out.exit_kind = ok ? EXIT_CONVERGED : EXIT_ABORT;
+    } else if (METHOD == 8) {
+        bool ok = prec1_phase(g, P.m, P.v.D, 2);  // ends with a barrier
+        if (ok && P.m.tile.on) {
+            tiles_init(g, P.m, P.v.D);
+            ok = grid_sync(g, 14);
+        }
+        if (ok) ok = ic_precond(g, P.m, P.v, P.cfg.ic_sweeps, P.v.r, P.v.z, [](int, T, T) {});
         out.exit_kind = ok ? EXIT_CONVERGED : EXIT_ABORT;
     } else if (METHOD == 2) {
         cgs_solve(g, P.m, P.v, P.cfg, out);

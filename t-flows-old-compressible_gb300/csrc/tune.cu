@@ -67,7 +67,8 @@ Key make_key(const DeviceTopology& t, const SolveRequest& rq) {
     const int rclass = (int)std::lround(2.0 * t.nnz / std::max(1, t.n));
     const int method = rq.method == 1 ? 0 : rq.method;
     const int prec = (rq.prec == 1 || rq.prec == 2) ? rq.prec : 0;
-    const int variant = rq.precision == 1 ? (rq.refine_restart ? 1 : 2) + 4 * rq.ic_bf16 : 0;
+    const int variant = (rq.precision == 1 ? (rq.refine_restart ? 1 : 2) + 4 * rq.ic_bf16 : 0) +
+                        8 * (tiled_ic(t, rq) ? 1 : 0);
     return Key(device_tag(t.device), rq.precision, method, prec, rq.ic_sweeps, variant, nclass,
                rclass, 0);
 }
@@ -206,7 +207,7 @@ int tune_solve(const DeviceTopology& t, Workspace& ws, const SolveRequest& rq, c
                 best.us_per_iter = us;
             }
         }
-    if (rq.prec == 2 && rq.ic_sweeps == 0) {
+    if (rq.prec == 2 && rq.ic_sweeps == 0 && !tiled_ic(t, rq)) {
         for (int sm : {2, 8}) {
             double us = 0.0;
             int grid = 0;
