@@ -437,7 +437,7 @@ def cfg1_latency(pkg, dev, reps=20):
 
 
 def ic_block(pkg, dev, n=128, iters=0, precisions=("fp64", "fp64_fma", "mixed"), tiled=(0, 1),
-             reps=2):
+             reps=2, blocks=(0,)):
     """IC(0)-preconditioned CG on the config-3 variable-density pressure
     system at n^3: per precision and per sweep kind (tiled / level-ordered),
     the time per iteration of the persistent solve (capped at `iters`
@@ -454,10 +454,10 @@ def ic_block(pkg, dev, n=128, iters=0, precisions=("fp64", "fp64_fma", "mixed"),
     mode = {"fp64": pkg.FP64, "fp64_fma": pkg.FP64_FMA, "mixed": pkg.MIXED}
     out = {"workload": f"{s.name}: CG + IC(0), tol 1e-8*||b|| (absolute), x0=0"
                        + (f", capped at {iters} iterations" if iters else ""), "n": s.N}
-    for label in precisions:
-        for t in tiled:
+    for label, t, blk in ((p, t, k) for p in precisions for t in tiled for k in blocks):
+        if True:
             kw = {"ic_bf16": 1} if label == "mixed" else {}
-            opts = pkg.options(precision=mode[label], ic_tiled=t, **kw)
+            opts = pkg.options(precision=mode[label], ic_tiled=t, block_size=blk, **kw)
             x.zero_()
             topo.solve(val, b, x, "cg", 2, maxit, s.tol, opts=opts, raise_on_error=False)
             torch.cuda.synchronize()
@@ -482,7 +482,8 @@ def ic_block(pkg, dev, n=128, iters=0, precisions=("fp64", "fp64_fma", "mixed"),
                 e1.record()
                 torch.cuda.synchronize()
                 rec["pivots_plus_apply_ms"] = e0.elapsed_time(e1) / reps
-            out[f"{label}_{'tiled' if t else 'level'}"] = rec
+            rec["block_size"] = r["block_size"]
+            out[f"{label}_{'tiled' if t else 'level'}" + (f"_b{blk}" if blk else "")] = rec
     topo.close()
     return out
 
@@ -773,6 +774,8 @@ def main():
                     help="--block ic: 1 tiled sweeps only, 0 level-ordered only, -1 both")
     ap.add_argument("--ic-precisions", default="fp64,fp64_fma,mixed",
                     help="--block ic: comma-separated precisions to time")
+    ap.add_argument("--ic-blocks", default="0",
+                    help="--block ic: comma-separated threads per block (0 = default)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -791,7 +794,9 @@ def main():
             tiled = (0, 1) if args.ic_tiled < 0 else (args.ic_tiled,)
             print(json.dumps(ic_block(pkg, dev, n=args.scale or 128, iters=args.ic_iters,
                                       precisions=tuple(args.ic_precisions.split(",")),
-                                      tiled=tiled, reps=1 if args.ic_iters else 2)), flush=True)
+                                      tiled=tiled, reps=1 if args.ic_iters else 2,
+                                      blocks=tuple(int(b) for b in args.ic_blocks.split(",")))),
+                  flush=True)
             return
         fn = {"calcps": assembly_block, "newuvw": momentum_block}[args.block]
         print(json.dumps(fn(pkg, dev, n=args.scale or 128)), flush=True)

@@ -509,6 +509,7 @@ cudaError_t fill_tiles(const DeviceTopology& t, Workspace& ws, const SolveReques
     tl.steps = tg.steps;
     tl.lu_bf16 = sizeof(L) == 2 ? 1 : 0;
     tl.recip = recip;
+    tl.half = tile_half(B, ls, sv);
     tl.rec_f = B * (3 * ls + (recip ? 3 : 2) * sv);
     tl.rec_b = B * (3 * ls + 3 * sv);
     tl.fwd = p;

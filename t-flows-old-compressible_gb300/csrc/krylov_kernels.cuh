@@ -55,7 +55,12 @@ enum : int { SLOT_A = 0, SLOT_B = 4, SLOT_C = 8, SLOT_D = 12, NUM_SLOTS = 16 };
 // build).  The cells of slot (k, s, t) = (k * steps + s) * block + t carry
 // the results a neighbouring tile reads.
 constexpr int kTileX = 16;     // tile width in x (columns per tile row)
-constexpr int kTileRing = 4;   // wavefront steps staged ahead in shared memory
+// The staged records form two halves of `half` steps each: one bulk copy
+// fills a half while the block works through the other.  The ring takes at
+// most kTileRingBytes of shared memory (so four 256-thread blocks still fit
+// on an SM) and a half at most kTileHalfMax steps.
+constexpr unsigned kTileRingBytes = 48u * 1024u;
+constexpr int kTileHalfMax = 4;
 
 template <typename T>
 struct Tiles {
@@ -66,6 +71,7 @@ struct Tiles {
     int steps;              // wavefront steps per tile: 16 + ty + nz - 2
     int lu_bf16;            // coefficients stored as BF16 bit patterns (FP32 solves)
     int recip;              // forward: mid = w * (1/(D+TINY)) instead of w / (D+TINY)
+    int half;               // steps per ring half (tile_half)
     unsigned rec_f, rec_b;  // bytes of one forward / backward record
     unsigned char* fwd;     // [tile][step] forward records
     unsigned char* bwd;     // [tile][step] backward records
@@ -74,15 +80,26 @@ struct Tiles {
 };
 
 // Bytes of one ring slot (the larger record: three coefficients and three
-// value fields), rounded to 128, and of the whole dynamic shared-memory block
-// of a tiled solve (barriers and flags, the ring, the neighbour exchange).
+// value fields), rounded to 128; steps per ring half; and the whole dynamic
+// shared-memory block of a tiled solve (barriers and flags, the ring, the
+// neighbour exchange).
 __host__ __device__ constexpr unsigned tile_slot_bytes(unsigned block, unsigned coef_bytes,
                                                        unsigned val_bytes) {
     return (block * (3 * coef_bytes + 3 * val_bytes) + 127u) / 128u * 128u;
 }
+__host__ __device__ constexpr int tile_half(unsigned block, unsigned coef_bytes, unsigned val_bytes) {
+    return kTileRingBytes / (2u * tile_slot_bytes(block, coef_bytes, val_bytes)) < 1u
+               ? 1
+               : (kTileRingBytes / (2u * tile_slot_bytes(block, coef_bytes, val_bytes)) >
+                          (unsigned)kTileHalfMax
+                      ? kTileHalfMax
+                      : (int)(kTileRingBytes / (2u * tile_slot_bytes(block, coef_bytes, val_bytes))));
+}
 __host__ __device__ constexpr unsigned tile_smem_bytes(unsigned block, unsigned coef_bytes,
                                                        unsigned val_bytes) {
-    return 128u + kTileRing * tile_slot_bytes(block, coef_bytes, val_bytes) + 2u * block * val_bytes;
+    return 128u + 2u * tile_half(block, coef_bytes, val_bytes) *
+                      tile_slot_bytes(block, coef_bytes, val_bytes) +
+           2u * block * val_bytes;
 }
 
 template <typename T>
@@ -668,21 +685,20 @@ __device__ bool ic_jacobi_apply(Grid& g, const Mat<T>& m, const T* D, const T* r
 // reference-arithmetic build the result is bit-identical to it and to the
 // level-ordered sweeps.
 //
-// Each step's record is staged into a ring of kTileRing shared-memory slots
-// by one bulk async copy issued kTileRing steps ahead (one elected thread,
-// one mbarrier per slot).  The right-hand side enters the forward records
+// The records are staged into a ring of two halves of `half` consecutive
+// steps each; one bulk async copy (one elected thread, one mbarrier per half)
+// fills a half while the block works through the other, so the issue cost is
+// paid once per `half` steps.  The right-hand side enters the forward records
 // through a gather each block runs for its own tiles before their first
 // step; the neighbour tiles' edge cells are loaded two steps ahead and
 // polled again only if they were not ready yet.
 
-constexpr int kTileCellAhead = 2;  // steps ahead for the neighbour edge cells
-
 struct TileSmem {
-    unsigned long long* bar;  // kTileRing barriers
+    unsigned long long* bar;  // two barriers, one per ring half
     volatile int* fail;       // set by a thread whose wait gave up
-    int* phase;               // ring slots' phase parities between sweeps
-    unsigned char* ring;
-    unsigned slot;            // bytes per ring slot
+    int* phase;               // the halves' phase parities between sweeps
+    unsigned char* ring;      // two halves of `half` records (at most tile_slot_bytes each)
+    unsigned slot;            // bytes of the largest record
 };
 
 template <typename T>
@@ -722,11 +738,14 @@ __device__ __forceinline__ T& tile_val(const Tiles<T>& tl, unsigned char* rec, i
     return reinterpret_cast<T*>(rec + tile_vfield(tl, v))[t];
 }
 
-// One record into a ring slot, completing on the slot's barrier.
-__device__ __forceinline__ void tile_issue(unsigned char* slot, unsigned long long* bar,
-                                           const unsigned char* rec, unsigned bytes) {
-    mbar_expect_tx(bar, bytes);
-    bulk_g2s(slot, rec, bytes, bar);
+// `count` consecutive records of `rec_bytes` each (a multiple of 128) into a
+// ring half, packed as they are in global memory: one copy, completing on
+// the half's barrier.
+__device__ __forceinline__ void tile_issue(unsigned char* dst, unsigned long long* bar,
+                                           const unsigned char* rec, unsigned rec_bytes,
+                                           int count) {
+    mbar_expect_tx(bar, rec_bytes * count);
+    bulk_g2s(dst, rec, rec_bytes * count, bar);
 }
 
 // A prefetched neighbour cell, polled again (bounded) while it still holds
@@ -751,12 +770,12 @@ __device__ __forceinline__ T tile_cell(const Grid& g, const TileSmem& sm, const 
     }
 }
 
-// Waits for a ring slot's copy (bounded).  False: abort raised, fail set.
-__device__ __forceinline__ bool tile_wait(const Grid& g, const TileSmem& sm, int u, unsigned parity,
+// Waits for a ring half's copy (bounded).  False: abort raised, fail set.
+__device__ __forceinline__ bool tile_wait(const Grid& g, const TileSmem& sm, int h, unsigned parity,
                                           int where) {
-    if (mbar_try_wait(sm.bar + u, parity)) return true;
+    if (mbar_try_wait(sm.bar + h, parity)) return true;
     const long long t0 = clock64();
-    while (!mbar_try_wait(sm.bar + u, parity)) {
+    while (!mbar_try_wait(sm.bar + h, parity)) {
         if (clock64() - t0 > g.timeout_cyc) {
             raise_abort(g.ctl, ST_TIMEOUT, where);
             *sm.fail = 1;
@@ -766,15 +785,15 @@ __device__ __forceinline__ bool tile_wait(const Grid& g, const TileSmem& sm, int
     return true;
 }
 
-// After a failure at step index j: thread 0 waits (bounded) for the copies
-// still in flight into the ring (steps j+1 .. j+kTileRing-1 of this tile).
-__device__ __forceinline__ void tile_drain(const Grid& g, const TileSmem& sm, int j, int S,
+// After a failure: thread 0 waits (bounded) for the copies still in flight
+// into the ring (the halves issued and not yet waited for, bits of `pend`).
+__device__ __forceinline__ void tile_drain(const Grid& g, const TileSmem& sm, unsigned pend,
                                            unsigned phase) {
     if (threadIdx.x != 0) return;
-    for (int jj = j + 1; jj < S && jj < j + kTileRing; ++jj) {
-        const int u = jj % kTileRing;
+    for (int h = 0; h < 2; ++h) {
+        if (!(pend & (1u << h))) continue;
         const long long t0 = clock64();
-        while (!mbar_try_wait(sm.bar + u, (phase >> u) & 1u))
+        while (!mbar_try_wait(sm.bar + h, (phase >> h) & 1u))
             if (clock64() - t0 > g.timeout_cyc) break;
     }
 }
@@ -806,7 +825,8 @@ __device__ void tiles_init(Grid& g, const Mat<T>& m, const T* __restrict__ D) {
     }
     const TileSmem sm = tile_smem(tl);
     if (threadIdx.x == 0) {
-        for (int u = 0; u < kTileRing; ++u) mbar_init(sm.bar + u, 1);
+        mbar_init(sm.bar, 1);
+        mbar_init(sm.bar + 1, 1);
         *sm.fail = 0;
         *sm.phase = 0;
         mbar_init_fence();
@@ -819,12 +839,12 @@ __device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs
     const Tiles<T>& tl = m.tile;
     const TileSmem sm = tile_smem(tl);
     const int B = blockDim.x, t = threadIdx.x, lx = t % kTileX, ly = t / kTileX;
-    const int S = tl.steps, ntiles = tl.ntx * tl.nty;
+    const int S = tl.steps, ntiles = tl.ntx * tl.nty, H = tl.half;
     const size_t plane = (size_t)S * B;
-    T* nbv = reinterpret_cast<T*>(sm.ring + kTileRing * sm.slot);
+    T* nbv = reinterpret_cast<T*>(sm.ring + 2 * H * sm.slot);
     const unsigned vf0 = tile_vfield(tl, 0), vf1 = tile_vfield(tl, 1), vf2 = tile_vfield(tl, 2);
     __syncthreads();
-    unsigned phase = (unsigned)*sm.phase;
+    unsigned phase = (unsigned)*sm.phase, pend = 0;
     bool ok = true;
     for (int k = g.bid; k < ntiles && ok; k += g.nblocks) {
         const int x = (k % tl.ntx) * kTileX + lx, y = (k / tl.ntx) * tl.ty + ly;
@@ -858,74 +878,80 @@ __device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs
             // and the previous tile's reads of the ring before the bulk copies
             fence_proxy_async_global();
             fence_proxy_async_smem();
-            for (int u = 0; u < kTileRing && u < S; ++u)
-                tile_issue(sm.ring + u * sm.slot, sm.bar + u, recf + (size_t)u * tl.rec_f, tl.rec_f);
+            for (int h = 0; h < 2 && h * H < S; ++h) {
+                tile_issue(sm.ring + h * H * tl.rec_f, sm.bar + h, recf + (size_t)h * H * tl.rec_f,
+                           tl.rec_f, min(H, S - h * H));
+                pend |= 1u << h;
+            }
         }
-        T xpre[kTileCellAhead], ypre[kTileCellAhead];
-        auto prefetch = [&](int s, T& xp, T& yp) {
+        // neighbour cells two steps ahead, by step parity
+        T xp0 = T(0), xp1 = T(0), yp0 = T(0), yp1 = T(0);
+        auto prefetch = [&](int s) {
             const int z = s - lx - ly;
             if (inb && z >= 0 && z < tl.nz) {
-                if (lx == 0 && x > 0) xp = Cell<T>::value(Cell<T>::load(xcell + (size_t)s * B));
-                if (ly == 0 && y > 0) yp = Cell<T>::value(Cell<T>::load(ycell + (size_t)s * B));
+                T xv = T(0), yv = T(0);
+                if (lx == 0 && x > 0) xv = Cell<T>::value(Cell<T>::load(xcell + (size_t)s * B));
+                if (ly == 0 && y > 0) yv = Cell<T>::value(Cell<T>::load(ycell + (size_t)s * B));
+                if (s & 1) { xp1 = xv; yp1 = yv; } else { xp0 = xv; yp0 = yv; }
             }
         };
-#pragma unroll
-        for (int u = 0; u < kTileCellAhead; ++u) {
-            xpre[u] = ypre[u] = T(0);
-            prefetch(u, xpre[u], ypre[u]);
-        }
+        prefetch(0);
+        if (S > 1) prefetch(1);
         T ycur = T(0);
-        for (int s0 = 0; s0 < S && ok; s0 += kTileRing) {
-#pragma unroll
-            for (int u = 0; u < kTileRing; ++u) {
-                const int s = s0 + u;
-                if (s >= S || !ok) break;
-                const int cu = u % kTileCellAhead;
-                tile_wait(g, sm, u, (phase >> u) & 1u, 26);
-                phase ^= 1u << u;
-                const int z = s - lx - ly;
-                if (inb && z >= 0 && z < tl.nz) {
-                    unsigned char* sl = sm.ring + u * sm.slot;
-                    const T ri = reinterpret_cast<const T*>(sl + vf1)[t];
-                    T acc = ri;
-                    if (z > 0) acc = acc - tile_coef(tl, sl, 0, t) * ycur;
-                    if (y > 0) {
-                        const T v = ly > 0 ? nbv[((s - 1) & 1) * B + t - kTileX]
-                                           : tile_cell(g, sm, ycell + (size_t)s * B, ypre[cu], 27);
-                        acc = acc - tile_coef(tl, sl, 1, t) * v;
-                    }
-                    if (x > 0) {
-                        const T v = lx > 0 ? nbv[((s - 1) & 1) * B + t - 1]
-                                           : tile_cell(g, sm, xcell + (size_t)s * B, xpre[cu], 27);
-                        acc = acc - tile_coef(tl, sl, 2, t) * v;
-                    }
-                    const T d = reinterpret_cast<const T*>(sl + vf0)[t];
-                    const T yv = acc * d;
-                    nbv[(s & 1) * B + t] = yv;
-                    ycur = yv;
-                    const size_t idx = base + (size_t)s * B + t;
-                    Cell<T>::store(tl.wt + idx, yv);
-                    // the middle step of CG.f90:144-146, for the backward sweep
-                    const T mid = tl.recip ? yv * reinterpret_cast<const T*>(sl + vf2)[t]
-                                           : yv / (d + tiny_v<T>());
-                    unsigned char* rb = recb + (size_t)s * tl.rec_b;
-                    reinterpret_cast<T*>(rb + vf1)[t] = mid;
-                    reinterpret_cast<T*>(rb + vf2)[t] = ri;
-                    tl.zt[idx] = Cell<T>::sentinel();
-                }
-                __syncthreads();
-                if (*sm.fail) {
-                    tile_drain(g, sm, s, S, phase);
-                    ok = false;
-                    break;
-                }
-                if (t == 0 && s + kTileRing < S) {
-                    fence_proxy_async_smem();  // the slot's reads before its refill
-                    tile_issue(sm.ring + u * sm.slot, sm.bar + u,
-                               recf + (size_t)(s + kTileRing) * tl.rec_f, tl.rec_f);
-                }
-                if (s + kTileCellAhead < S) prefetch(s + kTileCellAhead, xpre[cu], ypre[cu]);
+        for (int s = 0; s < S; ++s) {
+            const int u = s % (2 * H), hb = u / H;
+            if (u % H == 0) {
+                tile_wait(g, sm, hb, (phase >> hb) & 1u, 26);
+                phase ^= 1u << hb;
+                pend &= ~(1u << hb);
             }
+            const int z = s - lx - ly;
+            if (inb && z >= 0 && z < tl.nz) {
+                const unsigned char* sl = sm.ring + u * tl.rec_f;
+                const T ri = reinterpret_cast<const T*>(sl + vf1)[t];
+                T acc = ri;
+                if (z > 0) acc = acc - tile_coef(tl, sl, 0, t) * ycur;
+                if (y > 0) {
+                    const T v = ly > 0 ? nbv[((s - 1) & 1) * B + t - kTileX]
+                                       : tile_cell(g, sm, ycell + (size_t)s * B, (s & 1) ? yp1 : yp0, 27);
+                    acc = acc - tile_coef(tl, sl, 1, t) * v;
+                }
+                if (x > 0) {
+                    const T v = lx > 0 ? nbv[((s - 1) & 1) * B + t - 1]
+                                       : tile_cell(g, sm, xcell + (size_t)s * B, (s & 1) ? xp1 : xp0, 27);
+                    acc = acc - tile_coef(tl, sl, 2, t) * v;
+                }
+                const T d = reinterpret_cast<const T*>(sl + vf0)[t];
+                const T yv = acc * d;
+                nbv[(s & 1) * B + t] = yv;
+                ycur = yv;
+                const size_t idx = base + (size_t)s * B + t;
+                Cell<T>::store(tl.wt + idx, yv);
+                // the middle step of CG.f90:144-146, for the backward sweep
+                const T mid = tl.recip ? yv * reinterpret_cast<const T*>(sl + vf2)[t]
+                                       : yv / (d + tiny_v<T>());
+                unsigned char* rb = recb + (size_t)s * tl.rec_b;
+                reinterpret_cast<T*>(rb + vf1)[t] = mid;
+                reinterpret_cast<T*>(rb + vf2)[t] = ri;
+                tl.zt[idx] = Cell<T>::sentinel();
+            }
+            __syncthreads();
+            if (*sm.fail) {
+                tile_drain(g, sm, pend, phase);
+                ok = false;
+                break;
+            }
+            if (u % H == H - 1) {
+                // half hb consumed: refill it with the steps after the other half
+                const int first = s + 1 + H;
+                if (t == 0 && first < S) {
+                    fence_proxy_async_smem();  // the half's reads before its refill
+                    tile_issue(sm.ring + hb * H * tl.rec_f, sm.bar + hb,
+                               recf + (size_t)first * tl.rec_f, tl.rec_f, min(H, S - first));
+                    pend |= 1u << hb;
+                }
+            }
+            if (s + 2 < S) prefetch(s + 2);
         }
     }
     __syncthreads();
@@ -939,12 +965,12 @@ __device__ bool tile_backward(Grid& g, const Mat<T>& m, T* __restrict__ zout, Ep
     const Tiles<T>& tl = m.tile;
     const TileSmem sm = tile_smem(tl);
     const int B = blockDim.x, t = threadIdx.x, lx = t % kTileX, ly = t / kTileX;
-    const int S = tl.steps, ntiles = tl.ntx * tl.nty;
+    const int S = tl.steps, ntiles = tl.ntx * tl.nty, H = tl.half;
     const size_t plane = (size_t)S * B;
-    T* nbv = reinterpret_cast<T*>(sm.ring + kTileRing * sm.slot);
+    T* nbv = reinterpret_cast<T*>(sm.ring + 2 * H * sm.slot);
     const unsigned vf0 = tile_vfield(tl, 0), vf1 = tile_vfield(tl, 1), vf2 = tile_vfield(tl, 2);
     __syncthreads();
-    unsigned phase = (unsigned)*sm.phase;
+    unsigned phase = (unsigned)*sm.phase, pend = 0;
     if (t == 0) fence_proxy_async_global();  // the records written before the barrier
     bool ok = true;
     // this block's tiles (g.bid, g.bid + nblocks, ...) in decreasing order
@@ -960,79 +986,87 @@ __device__ bool tile_backward(Grid& g, const Mat<T>& m, T* __restrict__ zout, Ep
         const long long sb = (long long)base, sp = (long long)plane;
         const T* xcell = tl.zt + (sb + sp + ly * kTileX - (long long)(kTileX - 1) * B);
         const T* ycell = tl.zt + (sb + tl.ntx * sp + lx - (long long)(tl.ty - 1) * B);
+        // half h holds the steps of indices j in [h H, h H + H), j = S-1-s;
+        // they are the records S-1-j, in decreasing order, so the copy
+        // starts at the lowest step of the range and slot u holds step
+        // S-1-j at position (H-1-(j mod H)) from the half's start
+        auto issue = [&](int h, int j0) {
+            const int cnt = min(H, S - j0);
+            const int slo = S - 1 - (j0 + cnt - 1);  // lowest step of the range
+            tile_issue(sm.ring + (size_t)(h * H + H - cnt) * tl.rec_b, sm.bar + h,
+                       recb + (size_t)slo * tl.rec_b, tl.rec_b, cnt);
+            pend |= 1u << h;
+        };
         if (t == 0) {
             fence_proxy_async_smem();
-            for (int u = 0; u < kTileRing && u < S; ++u)
-                tile_issue(sm.ring + u * sm.slot, sm.bar + u, recb + (size_t)(S - 1 - u) * tl.rec_b,
-                           tl.rec_b);
+            for (int h = 0; h < 2 && h * H < S; ++h) issue(h, h * H);
         }
-        T xpre[kTileCellAhead], ypre[kTileCellAhead];
-        auto prefetch = [&](int s, T& xp, T& yp) {
-            const int z = s - lx - ly;
+        T xp0 = T(0), xp1 = T(0), yp0 = T(0), yp1 = T(0);
+        auto prefetch = [&](int j) {
+            const int s = S - 1 - j, z = s - lx - ly;
             if (inb && z >= 0 && z < tl.nz) {
+                T xv = T(0), yv = T(0);
                 if (lx == kTileX - 1 && x < tl.nx - 1)
-                    xp = Cell<T>::value(Cell<T>::load(xcell + (size_t)s * B));
+                    xv = Cell<T>::value(Cell<T>::load(xcell + (size_t)s * B));
                 if (ly == tl.ty - 1 && y < tl.ny - 1)
-                    yp = Cell<T>::value(Cell<T>::load(ycell + (size_t)s * B));
+                    yv = Cell<T>::value(Cell<T>::load(ycell + (size_t)s * B));
+                if (j & 1) { xp1 = xv; yp1 = yv; } else { xp0 = xv; yp0 = yv; }
             }
         };
-#pragma unroll
-        for (int u = 0; u < kTileCellAhead; ++u) {
-            xpre[u] = ypre[u] = T(0);
-            prefetch(S - 1 - u, xpre[u], ypre[u]);
-        }
+        prefetch(0);
+        if (S > 1) prefetch(1);
         T zcur = T(0);
-        for (int j0 = 0; j0 < S && ok; j0 += kTileRing) {
-#pragma unroll
-            for (int u = 0; u < kTileRing; ++u) {
-                const int j = j0 + u;
-                if (j >= S || !ok) break;
-                const int cu = u % kTileCellAhead;
-                const int s = S - 1 - j;
-                tile_wait(g, sm, u, (phase >> u) & 1u, 28);
-                phase ^= 1u << u;
-                const int z = s - lx - ly;
-                if (inb && z >= 0 && z < tl.nz) {
-                    const unsigned char* sl = sm.ring + u * sm.slot;
-                    const T d = reinterpret_cast<const T*>(sl + vf0)[t];
-                    T acc = reinterpret_cast<const T*>(sl + vf1)[t];  // mid
-                    const T ri = reinterpret_cast<const T*>(sl + vf2)[t];
-                    if (x < tl.nx - 1) {
-                        const T v = lx < kTileX - 1
-                                        ? nbv[((j - 1) & 1) * B + t + 1]
-                                        : tile_cell(g, sm, xcell + (size_t)s * B, xpre[cu], 29);
-                        acc = acc - tile_coef(tl, sl, 0, t) * v;
-                    }
-                    if (y < tl.ny - 1) {
-                        const T v = ly < tl.ty - 1
-                                        ? nbv[((j - 1) & 1) * B + t + kTileX]
-                                        : tile_cell(g, sm, ycell + (size_t)s * B, ypre[cu], 29);
-                        acc = acc - tile_coef(tl, sl, 1, t) * v;
-                    }
-                    if (z < tl.nz - 1) acc = acc - tile_coef(tl, sl, 2, t) * zcur;
-                    const T zi = acc * d;
-                    nbv[(j & 1) * B + t] = zi;
-                    zcur = zi;
-                    const size_t idx = base + (size_t)s * B + t;
-                    Cell<T>::store(tl.zt + idx, zi);
-                    tl.wt[idx] = Cell<T>::sentinel();
-                    const int row = x + tl.nx * (y + tl.ny * z);
-                    zout[row] = zi;
-                    epi(row, zi, ri);
-                }
-                __syncthreads();
-                if (*sm.fail) {
-                    tile_drain(g, sm, j, S, phase);
-                    ok = false;
-                    break;
-                }
-                if (t == 0 && j + kTileRing < S) {
-                    fence_proxy_async_smem();
-                    tile_issue(sm.ring + u * sm.slot, sm.bar + u,
-                               recb + (size_t)(s - kTileRing) * tl.rec_b, tl.rec_b);
-                }
-                if (j + kTileCellAhead < S) prefetch(s - kTileCellAhead, xpre[cu], ypre[cu]);
+        for (int j = 0; j < S; ++j) {
+            const int u = j % (2 * H), hb = u / H;
+            const int s = S - 1 - j;
+            if (u % H == 0) {
+                tile_wait(g, sm, hb, (phase >> hb) & 1u, 28);
+                phase ^= 1u << hb;
+                pend &= ~(1u << hb);
             }
+            const int z = s - lx - ly;
+            if (inb && z >= 0 && z < tl.nz) {
+                const unsigned char* sl = sm.ring + (size_t)(hb * H + (H - 1 - u % H)) * tl.rec_b;
+                const T d = reinterpret_cast<const T*>(sl + vf0)[t];
+                T acc = reinterpret_cast<const T*>(sl + vf1)[t];  // mid
+                const T ri = reinterpret_cast<const T*>(sl + vf2)[t];
+                if (x < tl.nx - 1) {
+                    const T v = lx < kTileX - 1
+                                    ? nbv[((j - 1) & 1) * B + t + 1]
+                                    : tile_cell(g, sm, xcell + (size_t)s * B, (j & 1) ? xp1 : xp0, 29);
+                    acc = acc - tile_coef(tl, sl, 0, t) * v;
+                }
+                if (y < tl.ny - 1) {
+                    const T v = ly < tl.ty - 1
+                                    ? nbv[((j - 1) & 1) * B + t + kTileX]
+                                    : tile_cell(g, sm, ycell + (size_t)s * B, (j & 1) ? yp1 : yp0, 29);
+                    acc = acc - tile_coef(tl, sl, 1, t) * v;
+                }
+                if (z < tl.nz - 1) acc = acc - tile_coef(tl, sl, 2, t) * zcur;
+                const T zi = acc * d;
+                nbv[(j & 1) * B + t] = zi;
+                zcur = zi;
+                const size_t idx = base + (size_t)s * B + t;
+                Cell<T>::store(tl.zt + idx, zi);
+                tl.wt[idx] = Cell<T>::sentinel();
+                const int row = x + tl.nx * (y + tl.ny * z);
+                zout[row] = zi;
+                epi(row, zi, ri);
+            }
+            __syncthreads();
+            if (*sm.fail) {
+                tile_drain(g, sm, pend, phase);
+                ok = false;
+                break;
+            }
+            if (u % H == H - 1) {
+                const int j0 = j + 1 + H;
+                if (t == 0 && j0 < S) {
+                    fence_proxy_async_smem();
+                    issue(hb, j0);
+                }
+            }
+            if (j + 2 < S) prefetch(j + 2);
         }
     }
     __syncthreads();
