@@ -750,8 +750,11 @@ __device__ __forceinline__ void tile_issue(unsigned char* dst, unsigned long lon
 
 // A prefetched neighbour cell, polled again (bounded) while it still holds
 // the sentinel.  On giving up: abort raised, the block's fail flag set.
+// (`ctl` and the limit `tmo` come as values: the sweeps keep everything
+// they use per step in registers.)
 template <typename T>
-__device__ __forceinline__ T tile_cell(const Grid& g, const TileSmem& sm, const T* p, T v, int where) {
+__device__ __forceinline__ T tile_cell(DevCtl* ctl, long long tmo, const TileSmem& sm, const T* p,
+                                       T v, int where) {
     using C = Cell<T>;
     if (C::bits(v) != C::kSentinel) return v;
     const long long t0 = clock64();
@@ -760,9 +763,9 @@ __device__ __forceinline__ T tile_cell(const Grid& g, const TileSmem& sm, const 
         const auto b = C::load(p);
         if (b != C::kSentinel) return C::value(b);
         if ((++spins & 63u) == 0u) {
-            const bool quit = ld_relaxed_s32(&g.ctl->abort) != 0;
-            if (quit || clock64() - t0 > g.timeout_cyc) {
-                if (!quit) raise_abort(g.ctl, ST_TIMEOUT, where);
+            const bool quit = ld_relaxed_s32(&ctl->abort) != 0;
+            if (quit || clock64() - t0 > tmo) {
+                if (!quit) raise_abort(ctl, ST_TIMEOUT, where);
                 *sm.fail = 1;
                 return T(0);
             }
@@ -771,13 +774,13 @@ __device__ __forceinline__ T tile_cell(const Grid& g, const TileSmem& sm, const 
 }
 
 // Waits for a ring half's copy (bounded).  False: abort raised, fail set.
-__device__ __forceinline__ bool tile_wait(const Grid& g, const TileSmem& sm, int h, unsigned parity,
-                                          int where) {
+__device__ __forceinline__ bool tile_wait(DevCtl* ctl, long long tmo, const TileSmem& sm, int h,
+                                          unsigned parity, int where) {
     if (mbar_try_wait(sm.bar + h, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(sm.bar + h, parity)) {
-        if (clock64() - t0 > g.timeout_cyc) {
-            raise_abort(g.ctl, ST_TIMEOUT, where);
+        if (clock64() - t0 > tmo) {
+            raise_abort(ctl, ST_TIMEOUT, where);
             *sm.fail = 1;
             return false;
         }
@@ -787,14 +790,14 @@ __device__ __forceinline__ bool tile_wait(const Grid& g, const TileSmem& sm, int
 
 // After a failure: thread 0 waits (bounded) for the copies still in flight
 // into the ring (the halves issued and not yet waited for, bits of `pend`).
-__device__ __forceinline__ void tile_drain(const Grid& g, const TileSmem& sm, unsigned pend,
+__device__ __forceinline__ void tile_drain(long long tmo, const TileSmem& sm, unsigned pend,
                                            unsigned phase) {
     if (threadIdx.x != 0) return;
     for (int h = 0; h < 2; ++h) {
         if (!(pend & (1u << h))) continue;
         const long long t0 = clock64();
         while (!mbar_try_wait(sm.bar + h, (phase >> h) & 1u))
-            if (clock64() - t0 > g.timeout_cyc) break;
+            if (clock64() - t0 > tmo) break;
     }
 }
 
@@ -836,7 +839,9 @@ __device__ void tiles_init(Grid& g, const Mat<T>& m, const T* __restrict__ D) {
 
 template <typename T>
 __device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs) {
-    const Tiles<T>& tl = m.tile;
+    const Tiles<T> tl = m.tile;  // a copy: the per-step fields stay in registers
+    DevCtl* const ctl = g.ctl;
+    const long long tmo = g.timeout_cyc;
     const TileSmem sm = tile_smem(tl);
     const int B = blockDim.x, t = threadIdx.x, lx = t % kTileX, ly = t / kTileX;
     const int S = tl.steps, ntiles = tl.ntx * tl.nty, H = tl.half;
@@ -898,60 +903,65 @@ __device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs
         prefetch(0);
         if (S > 1) prefetch(1);
         T ycur = T(0);
-        for (int s = 0; s < S; ++s) {
-            const int u = s % (2 * H), hb = u / H;
-            if (u % H == 0) {
-                tile_wait(g, sm, hb, (phase >> hb) & 1u, 26);
-                phase ^= 1u << hb;
-                pend &= ~(1u << hb);
-            }
-            const int z = s - lx - ly;
-            if (inb && z >= 0 && z < tl.nz) {
-                const unsigned char* sl = sm.ring + u * tl.rec_f;
-                const T ri = reinterpret_cast<const T*>(sl + vf1)[t];
-                T acc = ri;
-                if (z > 0) acc = acc - tile_coef(tl, sl, 0, t) * ycur;
-                if (y > 0) {
-                    const T v = ly > 0 ? nbv[((s - 1) & 1) * B + t - kTileX]
-                                       : tile_cell(g, sm, ycell + (size_t)s * B, (s & 1) ? yp1 : yp0, 27);
-                    acc = acc - tile_coef(tl, sl, 1, t) * v;
+        // one ring half per outer pass (no index arithmetic by a runtime
+        // divisor per step); a failed wait ends the tile at the half's end
+        int hb = 0;
+        for (int s0 = 0; s0 < S; s0 += H, hb ^= 1) {
+            tile_wait(ctl, tmo, sm, hb, (phase >> hb) & 1u, 26);
+            phase ^= 1u << hb;
+            pend &= ~(1u << hb);
+            const int cnt = min(H, S - s0);
+            const unsigned char* half = sm.ring + (size_t)hb * H * tl.rec_f;
+            for (int q = 0; q < cnt; ++q) {
+                const int s = s0 + q;
+                const int z = s - lx - ly;
+                if (inb && z >= 0 && z < tl.nz) {
+                    const unsigned char* sl = half + (size_t)q * tl.rec_f;
+                    const T ri = reinterpret_cast<const T*>(sl + vf1)[t];
+                    T acc = ri;
+                    if (z > 0) acc = acc - tile_coef(tl, sl, 0, t) * ycur;
+                    if (y > 0) {
+                        const T v = ly > 0 ? nbv[((s - 1) & 1) * B + t - kTileX]
+                                           : tile_cell(ctl, tmo, sm, ycell + (size_t)s * B,
+                                                       (s & 1) ? yp1 : yp0, 27);
+                        acc = acc - tile_coef(tl, sl, 1, t) * v;
+                    }
+                    if (x > 0) {
+                        const T v = lx > 0 ? nbv[((s - 1) & 1) * B + t - 1]
+                                           : tile_cell(ctl, tmo, sm, xcell + (size_t)s * B,
+                                                       (s & 1) ? xp1 : xp0, 27);
+                        acc = acc - tile_coef(tl, sl, 2, t) * v;
+                    }
+                    const T d = reinterpret_cast<const T*>(sl + vf0)[t];
+                    const T yv = acc * d;
+                    nbv[(s & 1) * B + t] = yv;
+                    ycur = yv;
+                    const size_t idx = base + (size_t)s * B + t;
+                    Cell<T>::store(tl.wt + idx, yv);
+                    // the middle step of CG.f90:144-146, for the backward sweep
+                    const T mid = tl.recip ? yv * reinterpret_cast<const T*>(sl + vf2)[t]
+                                           : yv / (d + tiny_v<T>());
+                    unsigned char* rb = recb + (size_t)s * tl.rec_b;
+                    reinterpret_cast<T*>(rb + vf1)[t] = mid;
+                    reinterpret_cast<T*>(rb + vf2)[t] = ri;
+                    tl.zt[idx] = Cell<T>::sentinel();
                 }
-                if (x > 0) {
-                    const T v = lx > 0 ? nbv[((s - 1) & 1) * B + t - 1]
-                                       : tile_cell(g, sm, xcell + (size_t)s * B, (s & 1) ? xp1 : xp0, 27);
-                    acc = acc - tile_coef(tl, sl, 2, t) * v;
-                }
-                const T d = reinterpret_cast<const T*>(sl + vf0)[t];
-                const T yv = acc * d;
-                nbv[(s & 1) * B + t] = yv;
-                ycur = yv;
-                const size_t idx = base + (size_t)s * B + t;
-                Cell<T>::store(tl.wt + idx, yv);
-                // the middle step of CG.f90:144-146, for the backward sweep
-                const T mid = tl.recip ? yv * reinterpret_cast<const T*>(sl + vf2)[t]
-                                       : yv / (d + tiny_v<T>());
-                unsigned char* rb = recb + (size_t)s * tl.rec_b;
-                reinterpret_cast<T*>(rb + vf1)[t] = mid;
-                reinterpret_cast<T*>(rb + vf2)[t] = ri;
-                tl.zt[idx] = Cell<T>::sentinel();
+                __syncthreads();
+                if (s + 2 < S) prefetch(s + 2);
             }
-            __syncthreads();
             if (*sm.fail) {
-                tile_drain(g, sm, pend, phase);
+                tile_drain(tmo, sm, pend, phase);
                 ok = false;
                 break;
             }
-            if (u % H == H - 1) {
-                // half hb consumed: refill it with the steps after the other half
-                const int first = s + 1 + H;
-                if (t == 0 && first < S) {
-                    fence_proxy_async_smem();  // the half's reads before its refill
-                    tile_issue(sm.ring + hb * H * tl.rec_f, sm.bar + hb,
-                               recf + (size_t)first * tl.rec_f, tl.rec_f, min(H, S - first));
-                    pend |= 1u << hb;
-                }
+            // this half consumed: refill it with the steps after the other half
+            const int first = s0 + 2 * H;
+            if (t == 0 && first < S) {
+                fence_proxy_async_smem();  // the half's reads before its refill
+                tile_issue(sm.ring + (size_t)hb * H * tl.rec_f, sm.bar + hb,
+                           recf + (size_t)first * tl.rec_f, tl.rec_f, min(H, S - first));
+                pend |= 1u << hb;
             }
-            if (s + 2 < S) prefetch(s + 2);
         }
     }
     __syncthreads();
@@ -962,7 +972,9 @@ __device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs
 
 template <typename T, typename Epi>
 __device__ bool tile_backward(Grid& g, const Mat<T>& m, T* __restrict__ zout, Epi epi) {
-    const Tiles<T>& tl = m.tile;
+    const Tiles<T> tl = m.tile;  // a copy: the per-step fields stay in registers
+    DevCtl* const ctl = g.ctl;
+    const long long tmo = g.timeout_cyc;
     const TileSmem sm = tile_smem(tl);
     const int B = blockDim.x, t = threadIdx.x, lx = t % kTileX, ly = t / kTileX;
     const int S = tl.steps, ntiles = tl.ntx * tl.nty, H = tl.half;
@@ -1016,57 +1028,61 @@ __device__ bool tile_backward(Grid& g, const Mat<T>& m, T* __restrict__ zout, Ep
         prefetch(0);
         if (S > 1) prefetch(1);
         T zcur = T(0);
-        for (int j = 0; j < S; ++j) {
-            const int u = j % (2 * H), hb = u / H;
-            const int s = S - 1 - j;
-            if (u % H == 0) {
-                tile_wait(g, sm, hb, (phase >> hb) & 1u, 28);
-                phase ^= 1u << hb;
-                pend &= ~(1u << hb);
-            }
-            const int z = s - lx - ly;
-            if (inb && z >= 0 && z < tl.nz) {
-                const unsigned char* sl = sm.ring + (size_t)(hb * H + (H - 1 - u % H)) * tl.rec_b;
-                const T d = reinterpret_cast<const T*>(sl + vf0)[t];
-                T acc = reinterpret_cast<const T*>(sl + vf1)[t];  // mid
-                const T ri = reinterpret_cast<const T*>(sl + vf2)[t];
-                if (x < tl.nx - 1) {
-                    const T v = lx < kTileX - 1
-                                    ? nbv[((j - 1) & 1) * B + t + 1]
-                                    : tile_cell(g, sm, xcell + (size_t)s * B, (j & 1) ? xp1 : xp0, 29);
-                    acc = acc - tile_coef(tl, sl, 0, t) * v;
+        int hb = 0;
+        for (int j0 = 0; j0 < S; j0 += H, hb ^= 1) {
+            tile_wait(ctl, tmo, sm, hb, (phase >> hb) & 1u, 28);
+            phase ^= 1u << hb;
+            pend &= ~(1u << hb);
+            const int cnt = min(H, S - j0);
+            // step S-1-(j0+q) sits at slot H-1-q of the half
+            const unsigned char* half = sm.ring + (size_t)(hb * H + H - 1) * tl.rec_b;
+            for (int q = 0; q < cnt; ++q) {
+                const int j = j0 + q;
+                const int s = S - 1 - j;
+                const int z = s - lx - ly;
+                if (inb && z >= 0 && z < tl.nz) {
+                    const unsigned char* sl = half - (size_t)q * tl.rec_b;
+                    const T d = reinterpret_cast<const T*>(sl + vf0)[t];
+                    T acc = reinterpret_cast<const T*>(sl + vf1)[t];  // mid
+                    const T ri = reinterpret_cast<const T*>(sl + vf2)[t];
+                    if (x < tl.nx - 1) {
+                        const T v = lx < kTileX - 1
+                                        ? nbv[((j - 1) & 1) * B + t + 1]
+                                        : tile_cell(ctl, tmo, sm, xcell + (size_t)s * B,
+                                                    (j & 1) ? xp1 : xp0, 29);
+                        acc = acc - tile_coef(tl, sl, 0, t) * v;
+                    }
+                    if (y < tl.ny - 1) {
+                        const T v = ly < tl.ty - 1
+                                        ? nbv[((j - 1) & 1) * B + t + kTileX]
+                                        : tile_cell(ctl, tmo, sm, ycell + (size_t)s * B,
+                                                    (j & 1) ? yp1 : yp0, 29);
+                        acc = acc - tile_coef(tl, sl, 1, t) * v;
+                    }
+                    if (z < tl.nz - 1) acc = acc - tile_coef(tl, sl, 2, t) * zcur;
+                    const T zi = acc * d;
+                    nbv[(j & 1) * B + t] = zi;
+                    zcur = zi;
+                    const size_t idx = base + (size_t)s * B + t;
+                    Cell<T>::store(tl.zt + idx, zi);
+                    tl.wt[idx] = Cell<T>::sentinel();
+                    const int row = x + tl.nx * (y + tl.ny * z);
+                    zout[row] = zi;
+                    epi(row, zi, ri);
                 }
-                if (y < tl.ny - 1) {
-                    const T v = ly < tl.ty - 1
-                                    ? nbv[((j - 1) & 1) * B + t + kTileX]
-                                    : tile_cell(g, sm, ycell + (size_t)s * B, (j & 1) ? yp1 : yp0, 29);
-                    acc = acc - tile_coef(tl, sl, 1, t) * v;
-                }
-                if (z < tl.nz - 1) acc = acc - tile_coef(tl, sl, 2, t) * zcur;
-                const T zi = acc * d;
-                nbv[(j & 1) * B + t] = zi;
-                zcur = zi;
-                const size_t idx = base + (size_t)s * B + t;
-                Cell<T>::store(tl.zt + idx, zi);
-                tl.wt[idx] = Cell<T>::sentinel();
-                const int row = x + tl.nx * (y + tl.ny * z);
-                zout[row] = zi;
-                epi(row, zi, ri);
+                __syncthreads();
+                if (j + 2 < S) prefetch(j + 2);
             }
-            __syncthreads();
             if (*sm.fail) {
-                tile_drain(g, sm, pend, phase);
+                tile_drain(tmo, sm, pend, phase);
                 ok = false;
                 break;
             }
-            if (u % H == H - 1) {
-                const int j0 = j + 1 + H;
-                if (t == 0 && j0 < S) {
-                    fence_proxy_async_smem();
-                    issue(hb, j0);
-                }
+            const int jn = j0 + 2 * H;
+            if (t == 0 && jn < S) {
+                fence_proxy_async_smem();
+                issue(hb, jn);
             }
-            if (j + 2 < S) prefetch(j + 2);
         }
     }
     __syncthreads();
