@@ -437,7 +437,7 @@ def cfg1_latency(pkg, dev, reps=20):
 
 
 def ic_block(pkg, dev, n=128, iters=0, precisions=("fp64", "fp64_fma", "mixed"), tiled=(0, 1),
-             reps=2, blocks=(0,)):
+             reps=2, blocks=(0,), restart=None):
     """IC(0)-preconditioned CG on the config-3 variable-density pressure
     system at n^3: per precision and per sweep kind (tiled / level-ordered),
     the time per iteration of the persistent solve (capped at `iters`
@@ -457,6 +457,8 @@ def ic_block(pkg, dev, n=128, iters=0, precisions=("fp64", "fp64_fma", "mixed"),
     for label, t, blk in ((p, t, k) for p in precisions for t in tiled for k in blocks):
         if True:
             kw = {"ic_bf16": 1} if label == "mixed" else {}
+            if label == "mixed" and restart is not None:
+                kw["refine_restart"] = restart
             opts = pkg.options(precision=mode[label], ic_tiled=t, block_size=blk, **kw)
             x.zero_()
             topo.solve(val, b, x, "cg", 2, maxit, s.tol, opts=opts, raise_on_error=False)
@@ -774,6 +776,8 @@ def main():
                     help="--block ic: 1 tiled sweeps only, 0 level-ordered only, -1 both")
     ap.add_argument("--ic-precisions", default="fp64,fp64_fma,mixed",
                     help="--block ic: comma-separated precisions to time")
+    ap.add_argument("--ic-restart", type=int, default=None,
+                    help="--block ic: mixed refinement, 1 restarted, 0 reliable updates")
     ap.add_argument("--ic-blocks", default="0",
                     help="--block ic: comma-separated threads per block (0 = default)")
     args = ap.parse_args()
@@ -795,7 +799,8 @@ def main():
             print(json.dumps(ic_block(pkg, dev, n=args.scale or 128, iters=args.ic_iters,
                                       precisions=tuple(args.ic_precisions.split(",")),
                                       tiled=tiled, reps=1 if args.ic_iters else 2,
-                                      blocks=tuple(int(b) for b in args.ic_blocks.split(",")))),
+                                      blocks=tuple(int(b) for b in args.ic_blocks.split(",")),
+                                      restart=args.ic_restart)),
                   flush=True)
             return
         fn = {"calcps": assembly_block, "newuvw": momentum_block}[args.block]

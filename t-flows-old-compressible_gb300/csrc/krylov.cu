@@ -45,21 +45,28 @@ __global__ void to_double_kernel(const float* __restrict__ a, double* __restrict
 
 // SELL values from stored-order values: one thread per row.  With `tpos`
 // the values of A^T in A's pattern (entry (i,j) <- stored entry (j,i)).
-// `s16` receives BF16 bit patterns, rounded to nearest even from FP64.
-__global__ void permute_kernel(int n, const int* __restrict__ rowptr,
+// `s16` receives BF16 bit patterns, rounded to nearest even from FP64.  The
+// FP32 copy `s32` holds the row sum (in FP64, rounded) in the diagonal slot:
+// its products run in difference form (sell_row).
+__global__ void permute_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
                                const long long* __restrict__ soff, const double* __restrict__ val,
                                double* __restrict__ s64, float* __restrict__ s32,
                                unsigned short* __restrict__ s16, const int* __restrict__ tpos) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int b = rowptr[i], e = rowptr[i + 1];
         const long long base = soff[i >> 5] + (i & 31);
+        double rowsum = 0.0;
         for (int j = b; j < e; ++j) {
             const double a = tpos ? val[tpos[j]] : val[j];
             const long long o = base + 32LL * (j - b);
+            rowsum += a;
             if (s64) s64[o] = a;
             if (s32) s32[o] = (float)a;
             if (s16) s16[o] = __bfloat16_as_ushort(__double2bfloat16(a));
         }
+        if (s32)
+            for (int j = b; j < e; ++j)
+                if (col[j] == i) s32[base + 32LL * (j - b)] = (float)rowsum;
     }
 }
 
@@ -282,7 +289,7 @@ cudaError_t permute_values(const DeviceTopology& t, Workspace& ws, const double*
                            bool want64, bool want32, cudaStream_t s, bool want16) {
     if (want16 && !ws.sval16) return cudaErrorInvalidValue;  // ensure_lu16 first
     const int nb = std::min(std::max(1, (t.n + 255) / 256), sms() * 16);
-    permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.soff, csr_val, want64 ? ws.sval64 : nullptr,
+    permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.col, t.soff, csr_val, want64 ? ws.sval64 : nullptr,
                                       want32 ? ws.sval32 : nullptr, want16 ? ws.sval16 : nullptr,
                                       nullptr);
     return cudaGetLastError();
@@ -301,7 +308,7 @@ cudaError_t permute_transposed(const DeviceTopology& t, Workspace& ws, const dou
         if (e != cudaSuccess) return e;
     }
     const int nb = std::min(std::max(1, (t.n + 255) / 256), sms() * 16);
-    permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.soff, csr_val, ws.svalT64, nullptr, nullptr,
+    permute_kernel<<<nb, 256, 0, s>>>(t.n, t.rowptr, t.col, t.soff, csr_val, ws.svalT64, nullptr, nullptr,
                                       t.tpos);
     return cudaGetLastError();
 }

@@ -254,15 +254,35 @@ __device__ __forceinline__ void sell_cols8(const Mat<T>& m, int s, int lane, int
     }
 }
 
-// q_i = sum_j a_ij x_j over row i = 32*s + lane, left to right from 0.  Rows
-// of at most 8 stored entries (every hex or prism cell) take a fully
-// unrolled path: all index and value loads issue before the gathers.
+// FP32 products in difference form.  The FP32 copy of a matrix keeps its
+// off-diagonal entries rounded to FP32 but holds, in the diagonal slot, the
+// row sum c_i (summed in FP64, then rounded); a product is then formed as
+//     q_i = c_i x_i + sum_{j != i} a_ij (x_j - x_i),
+// the same number in exact arithmetic.  Rounding each entry separately would
+// perturb every row sum by ~6e-8 |a_ii|; for the pressure-correction
+// operator -- a graph Laplacian whose rows sum to zero except at Dirichlet
+// cells -- that shifts the smallest eigenvalues, so FP32 inner CG iterations
+// converge towards a different operator and each FP64 refinement pays for
+// it (measured: 112 instead of 84 iterations at 24^3; reliable updates
+// stalling at 256^3).  In difference form the rounding error of a product
+// scales with the variation of x, and the near null space of the operator
+// (smooth x) is kept.  The FP64 matrices keep the reference's plain sums.
+template <typename T>
+__device__ __forceinline__ T diff_term(T a, T xj, T xi, bool diag) {
+    return diag ? a * xi : a * (xj - xi);
+}
+
+// q_i = sum_j a_ij x_j over row i = 32*s + lane, left to right from 0 (FP32:
+// in difference form).  Rows of at most 8 stored entries (every hex or prism
+// cell) take a fully unrolled path: all index and value loads issue before
+// the gathers.
 template <typename T, typename X>
 __device__ __forceinline__ T sell_row(const Mat<T>& m, int s, int lane, const X* __restrict__ xv) {
     const long long b0 = m.soff[s];
     const int w = (int)((m.soff[s + 1] - b0) >> 5);
     const int* cp = m.scol + b0 + lane;
     const T* vp = m.sval + b0 + lane;
+    const int i = s * kWarp + lane;
     T acc = T(0);
     if (w <= 8) {
         int c[8];
@@ -272,9 +292,27 @@ __device__ __forceinline__ T sell_row(const Mat<T>& m, int s, int lane, const X*
         for (int t = 0; t < 8; ++t) v[t] = t < w ? vp[32 * t] : T(0);
 #pragma unroll
         for (int t = 0; t < 8; ++t) xx[t] = c[t] >= 0 ? T(xv[c[t]]) : T(0);
+        if constexpr (sizeof(T) == 4) {
+            T xi = T(0);
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                if (c[t] == i) xi = xx[t];
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                if (c[t] >= 0) acc = acc + diff_term(v[t], xx[t], xi, c[t] == i);
+            return acc;
+        }
 #pragma unroll
         for (int t = 0; t < 8; ++t)
             if (c[t] >= 0) acc = acc + v[t] * xx[t];
+        return acc;
+    }
+    if constexpr (sizeof(T) == 4) {
+        const T xi = i < m.n ? T(xv[i]) : T(0);
+        for (int t = 0; t < w; ++t) {
+            const int c = cp[32 * t];
+            if (c >= 0) acc = acc + diff_term(vp[32 * t], T(xv[c]), xi, c == i);
+        }
         return acc;
     }
     for (int t = 0; t < w; ++t) {
@@ -317,22 +355,34 @@ __device__ __forceinline__ float sell_row_dir(const Mat<float>& m, int s, int la
             zz[t] = c[t] >= 0 ? z[c[t]] : 0.f;
             pp[t] = c[t] >= 0 && !first ? p[c[t]] : 0.f;
         }
+        // difference form (see sell_row): the row's own direction first
+        const int i = s * kWarp + lane;
+        float di = 0.f;
 #pragma unroll
         for (int t = 0; t < 8; ++t)
-            if (c[t] >= 0) acc = acc + v[t] * fused_dir(zz[t], beta, pp[t], first);
+            if (c[t] == i) di = fused_dir(zz[t], beta, pp[t], first);
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (c[t] >= 0) acc = acc + diff_term(v[t], fused_dir(zz[t], beta, pp[t], first), di, c[t] == i);
         return acc;
     }
+    const int i = s * kWarp + lane;
+    const float di = i < m.n ? fused_dir(z[i], beta, first ? 0.f : p[i], first) : 0.f;
     for (int t = 0; t < w; ++t) {
         const int c = cp[32 * t];
-        if (c >= 0) acc = acc + vp[32 * t] * fused_dir(z[c], beta, first ? 0.f : p[c], first);
+        if (c >= 0)
+            acc = acc + diff_term(vp[32 * t], fused_dir(z[c], beta, first ? 0.f : p[c], first), di,
+                                  c == i);
     }
     return acc;
 }
 
-// r_i <- r_i - a_i1 x_1 - a_i2 x_2 - ... (Process/Resid.f90:28-33 order).
+// r_i <- r_i - a_i1 x_1 - a_i2 x_2 - ... (Process/Resid.f90:28-33 order;
+// FP32: r_i - (the difference-form product)).
 template <typename T, typename X>
 __device__ __forceinline__ T sell_resid_row(const Mat<T>& m, int s, int lane, T ri,
                                             const X* __restrict__ xv) {
+    if constexpr (sizeof(T) == 4) return ri - sell_row(m, s, lane, xv);
     const long long b0 = m.soff[s];
     const int w = (int)((m.soff[s + 1] - b0) >> 5);
     const int* cp = m.scol + b0 + lane;
