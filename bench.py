@@ -1,26 +1,38 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 Krylov solver core.
 
-Metric: time to a 1e-8 relative residual of the T-FlowS solvers, reported as
-whole-job solves/s (higher is better), with the HBM bandwidth the solver
-kernel achieves.  Default workload: 128^3 perturbed-hex convection-diffusion
-system (momentum / scalar transport), BiCG with diagonal preconditioning in
-FP64 with fused multiply-adds (--precision fp64 for the reference's own
-arithmetic), the reference's convergence test (absolute tolerance
-1e-8*||b||), x0 = 0.  Synthetic data (seeded); the matrix and vectors
-(~260 MB) exceed the 129 MB L2, so no flush is needed between steps.
+Metric: time to a 1e-8 residual of the T-FlowS solvers, mixed precision
+against FP64, as whole-job solves/s (higher is better), with the HBM
+bandwidth the solver kernel achieves.
+
+Headline workload (the metric's own configuration): the 256^3 perturbed-hex
+variable-density pressure-correction system (density ratio 7), CG with
+IC(0) preconditioning, mixed precision -- FP32 SpMV and vectors, BF16
+off-diagonal IC factors with FP32 pivots, exact triangular sweeps -- inside
+FP64 iterative refinement, to the reference's test ||r|| < 1e-8*||b||,
+x0 = 0.  The same line carries the like-for-like comparison: the same method
+and preconditioner on the fastest FP64 build (fused multiply-adds), the
+reference-arithmetic FP64 build, and the diagonal and Jacobi-sweep IC
+variants, each with its iteration count and its error against a tight FP64
+solve (||r|| <= 1e-12*||b||).  Synthetic seeded data (mesh.py documents it;
+the reference uses no public dataset); the 2 GB of matrix and vectors exceed
+the 129 MB L2, so no flush is needed between steps.
 
 A "step" is one complete solve.  `value` times K solves on data resident in
-HBM (device API); `e2e` times K calls of the Fortran-facing C ABI
-(tflows_bicg) with the matrix, x and b in pinned host memory, host<->device
-copies inside each call.  The CPU baseline is the oracle (the reference's
-algorithm restated in C) on the host cores.
+HBM (device API); `e2e` times K calls of the Fortran-facing C ABI (tflows_cg
+with the mixed-precision options set) with the matrix, x and b in pinned
+host memory, host<->device copies inside each call.  The CPU baseline is the
+oracle (the reference's algorithm restated in C) on the host cores: a full
+256^3 IC(0) solve takes tens of minutes on one core, so each sample times
+the solve's set-up and a few whole iterations and scales them by the
+iteration count of one committed full run (oracle/cfg3_256cube_full_solve.json).
 
 Multi-GPU: the solves are independent replicas (one per rank, no
 collective); value = total solves / max-over-ranks time.
 
 --impl reference: the reference algorithm (oracle port, FP64, serial per
-solve as in the reference) on the host cores, one solve per core at a time.
+solve as in the reference) on every host core, one solve per core at a time,
+on the same workload, scaled the same way.
 """
 from __future__ import annotations
 
@@ -168,54 +180,127 @@ def cpu_reference_throughput(s, method, prec, threads, seconds_budget):
     return sum(done) / el, sum(done), its[0], el
 
 
+FULL_RUN = os.path.join(ROOT, "oracle", "cfg3_256cube_full_solve.json")
+
+
+def oracle_full_iterations(s, method, prec):
+    """Iterations of the committed full oracle solve of this workload, or
+    None when no committed run matches it."""
+    try:
+        with open(FULL_RUN) as f:
+            d = json.load(f)
+        if d["workload"] == s.name and d["method"] == method and d["prec"] == prec:
+            return int(d["iterations"])
+    except Exception:
+        pass
+    return None
+
+
+class OracleSampler:
+    """The oracle on `threads` host threads, each running the same solve
+    concurrently (one per core, as the reference runs one solve per MPI
+    rank).  A sample times the set-up (Prec1, ||b||, Resid) and `iters` whole
+    iterations; the time of a full solve is the set-up plus the full run's
+    iteration count times the measured time per iteration."""
+
+    def __init__(self, s, method, prec, threads, iters, fallback_iterations=None):
+        import oracle
+        oracle.build()
+        self.s, self.method, self.prec, self.threads, self.iters = s, method, prec, threads, iters
+        self.full_it = oracle_full_iterations(s, method, prec)
+        self.full_it_source = "committed full oracle run"
+        if self.full_it is None and (s.N <= 300000 or not fallback_iterations):
+            # small workloads (tests): one full solve gives the count
+            _, _, self.full_it, _, _ = oracle.solve(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow,
+                                                    s.Adia, s.Ab, s.x, s.b, prec, 20000, s.tol)
+            self.full_it_source = "full oracle solve in this run"
+        elif self.full_it is None:
+            # the reference-arithmetic GPU solve runs the same algorithm
+            self.full_it = int(fallback_iterations)
+            self.full_it_source = "iterations of the reference-arithmetic GPU solve"
+        self.t_setup = self.run(0)
+
+    def run(self, iters):
+        import oracle
+        s = self.s
+
+        def work():
+            oracle.solve(self.method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab, s.x,
+                         s.b, self.prec, iters, s.tol)
+
+        ths = [threading.Thread(target=work) for _ in range(self.threads)]
+        t0 = time.perf_counter()
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        return time.perf_counter() - t0
+
+    def sample(self):
+        """One sample: (solves/s over all threads, seconds of the sample,
+        estimated seconds of one full solve)."""
+        t = self.run(self.iters)
+        t_iter = max(t - self.t_setup, 1e-9) / max(self.iters, 1)
+        t_full = self.t_setup + self.full_it * t_iter
+        return self.threads / t_full, t, t_full
+
+    def describe(self, elapsed):
+        return (f"{self.threads} concurrent oracle solves of the workload (one per thread), "
+                f"each timed over its set-up ({self.t_setup:.2f} s) and {self.iters} whole "
+                f"iterations, scaled to {self.full_it} iterations ({self.full_it_source}); "
+                f"{elapsed:.1f} s of sampling")
+
+
 def run_reference(args):
     import __graft_entry__ as ge
     rank, world, _ = dist_env()
     if rank != 0:
         return
     pkg = ge.load_package()
-    s = pkg.mesh.config_system(2)
+    s = make_workload(pkg, args.workload, args.scale)
+    method, prec = args.method, args.prec
     cores = os.cpu_count() or 1
-    # W warm-up steps and K timed steps; each step is one round of
-    # concurrent solves (one per core).
-    import oracle
-    oracle.build()
+    sampler = OracleSampler(s, method, prec, cores, args.oracle_iters)
     for _ in range(args.warmup):
-        cpu_reference_throughput(s, "bicg", 1, cores, 0.0)
+        sampler.sample()
     t0 = time.perf_counter()
-    total = 0
-    it = 0
+    vals = []
+    t_full = 0.0
     for _ in range(args.steps):
-        _, n, it, _ = cpu_reference_throughput(s, "bicg", 1, cores, 0.0)
-        total += n
+        v, _, t_full = sampler.sample()
+        vals.append(v)
     el = time.perf_counter() - t0
-    value = total / el
+    value = statistics.median(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(s, "bicg", 1),
+        "config": workload_config(s, method, prec),
         "arithmetic": "FP64 as the reference (oracle C restatement, no fused multiply-adds)",
+        "full_solve_seconds_per_core": t_full,
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} concurrent full BiCG solves per step "
-                                   f"({it} iterations each), oracle C restatement, 1 thread each"},
+                         "sample": sampler.describe(el)},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def workload_config(s, method, prec):
-    return {"workload": f"{s.name}: {method} solve to 1e-8*||b|| (absolute test as the "
-                        f"reference), x0=0, prec {prec}",
-            "n": s.N, "nnz": s.nnz, "method": method, "prec": prec,
-            "l2": "inputs larger than L2 (no flush)"}
+def workload_config(s, method, prec, precision=None):
+    c = {"workload": f"{s.name}: {method} solve to 1e-8*||b|| (absolute test as the "
+                     f"reference), x0=0, prec {prec}",
+         "n": s.N, "nnz": s.nnz, "method": method, "prec": prec,
+         "l2": "inputs larger than L2 (no flush)"}
+    if precision:
+        c["precision"] = precision
+    return c
 
 
 ARITHMETIC = {"fp64": "FP64, reference arithmetic (separate rounded products and sums)",
               "fp64_fma": "FP64 with fused multiply-adds and a reciprocal diagonal",
-              "mixed": "FP32 inner solves, FP64 refinement"}
+              "mixed": "FP32 inner solves (FP32 SpMV in difference form and FP32 vectors), "
+                       "FP64 residual and refinement"}
 
 
 def make_workload(pkg, name, scale):
@@ -248,59 +333,67 @@ def device_solves(pkg, topo, val, b, x, method, prec, tol, opts, steps, warmup, 
     return e0.elapsed_time(e1) * 1e-3, out
 
 
-IC_VARIANTS = (("exact_fp32", {}), ("exact_bf16", {"ic_bf16": 1}),
-               ("jacobi1_bf16", {"ic_sweeps": 1, "ic_bf16": 1}),
-               ("jacobi2_bf16", {"ic_sweeps": 2, "ic_bf16": 1}),
-               ("jacobi2_fp32", {"ic_sweeps": 2}),
-               ("jacobi4_bf16", {"ic_sweeps": 4, "ic_bf16": 1}))
+# The like-for-like rows of the config-3 comparison: (label, precision,
+# prec, IC options).  Mixed rows use BF16 factor entries; each mixed row has
+# an FP64 row with the same preconditioner on the fastest FP64 build.
+CFG3_ROWS = (("fp64_fma_ic_exact", "fp64_fma", 2, {}),
+             ("fp64_ic_exact", "fp64", 2, {}),
+             ("mixed_diag", "mixed", 1, {}),
+             ("fp64_fma_diag", "fp64_fma", 1, {}),
+             ("mixed_ic_jacobi1_bf16", "mixed", 2, {"ic_sweeps": 1, "ic_bf16": 1}),
+             ("fp64_fma_ic_jacobi1", "fp64_fma", 2, {"ic_sweeps": 1}),
+             ("mixed_ic_jacobi2_bf16", "mixed", 2, {"ic_sweeps": 2, "ic_bf16": 1}),
+             ("fp64_fma_ic_jacobi2", "fp64_fma", 2, {"ic_sweeps": 2}))
+PAIRS = (("ic_exact", "mixed_ic_exact_bf16", "fp64_fma_ic_exact", "fp64_ic_exact"),
+         ("diag", "mixed_diag", "fp64_fma_diag", None),
+         ("ic_jacobi1", "mixed_ic_jacobi1_bf16", "fp64_fma_ic_jacobi1", None),
+         ("ic_jacobi2", "mixed_ic_jacobi2_bf16", "fp64_fma_ic_jacobi2", None))
 
 
-def mixed_vs_fp64(pkg, dev, scale, precs, reps):
-    """The variable-density pressure system (cfg3): CG with each given
-    preconditioner in FP64 (reference arithmetic) and in mixed precision
-    (FP32 inner solves, FP64 refinement), same absolute tolerance.  With
-    IC(0) the mixed solve is run with each factor variant (FP32 or BF16
-    factor entries, exact triangular solves or k Jacobi sweeps)."""
+def precision_mode(pkg, name):
+    return {"fp64": pkg.FP64, "fp64_fma": pkg.FP64_FMA, "mixed": pkg.MIXED}[name]
+
+
+def cfg3_comparison(pkg, dev, topo, s, val, b, headline, x_head, reps=1):
+    """Every row of CFG3_ROWS on the headline system (each with its own tuned
+    launch shape, tuned on a first untimed solve), the headline's own result,
+    and for each the relative error max|x - x*| / max|x*| against a tight FP64
+    solve x* (FP64-FMA, exact IC, ||r|| <= 1e-12*||b||); speed-ups of each
+    mixed row over its FP64 rows with the same preconditioner."""
     import torch
-    s = make_workload(pkg, "cfg3", scale)
-    topo = pkg.Topology.from_system(s)
-    val = torch.from_numpy(s.A[:-1].copy()).to(dev)
-    b = torch.from_numpy(s.b.copy()).to(dev)
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
+    tight = pkg.options(precision=pkg.FP64_FMA, tol_mode=pkg.TOL_RELATIVE, autotune=1)
+    res = topo.solve(val, b, x, "cg", 2, 20000, 1e-12, opts=tight)
+    x_star = x.clone()
+    scale = float(x_star.abs().max())
+    out = {"tight_reference": {"what": "FP64-FMA CG + exact IC(0) to ||r|| <= 1e-12*||b||",
+                               "iterations": res["iterations"], "status": res["status"]}}
 
-    def run(prec, opts):
-        # every variant runs with its own tuned launch shape (tuned on the
-        # first, untimed solve)
-        opts.autotune = 1
-        el, out = device_solves(pkg, topo, val, b, x, "cg", prec, s.tol, opts, reps, 1)
-        r = out[-1]
-        return {"ms": 1e3 * el / reps, "iterations": r["iterations"],
-                "refinements": r["refinements"], "fin_res": r["fin_res"],
-                "gbs": r["bytes"] / r["seconds"] / 1e9, "status": r["status"],
-                "block_size": r["block_size"], "grid_blocks": r["grid_blocks"]}, x.clone()
+    def err(xv):
+        return float((xv - x_star).abs().max()) / scale
 
-    result = {}
-    for prec in precs:
-        fp, x64 = run(prec, pkg.options(precision=pkg.FP64))
-        fpf, _ = run(prec, pkg.options(precision=pkg.FP64_FMA))
-        variants = IC_VARIANTS if prec == 2 else (("jacobi_fp32", {}),)
-        mixed = {}
-        for label, kw in variants:
-            rec, xm = run(prec, pkg.options(precision=pkg.MIXED, **kw))
-            rec["rel_diff_vs_fp64"] = float((xm - x64).abs().max() / x64.abs().max())
-            mixed[label] = rec
-        ok = [k for k in mixed if mixed[k]["status"] == pkg.OK] or list(mixed)
-        best = min(ok, key=lambda k: mixed[k]["ms"])
-        result[prec] = {"workload": f"{s.name}, CG prec {prec}, tol 1e-8*||b|| absolute",
-                        "n": s.N, "fp64": fp, "fp64_fma": fpf, "mixed": mixed[best],
-                        "mixed_variant": best,
-                        "speedup": fp["ms"] / mixed[best]["ms"],
-                        "speedup_vs_fp64_fma": fpf["ms"] / mixed[best]["ms"],
-                        "mixed_rel_diff_vs_fp64": mixed[best]["rel_diff_vs_fp64"]}
-        if len(mixed) > 1:
-            result[prec]["all_mixed_variants"] = mixed
-    topo.close()
-    return result
+    head = dict(headline)
+    head["rel_err_vs_tight_fp64"] = err(x_head)
+    out["mixed_ic_exact_bf16"] = head
+    for label, prec_name, prec, ic in CFG3_ROWS:
+        opts = pkg.options(precision=precision_mode(pkg, prec_name), autotune=1, **ic)
+        el, rr = device_solves(pkg, topo, val, b, x, "cg", prec, s.tol, opts, reps, 1)
+        r = rr[-1]
+        out[label] = {"ms": 1e3 * el / reps, "iterations": r["iterations"],
+                      "inner_iterations": r["inner_iterations"], "refinements": r["refinements"],
+                      "fin_res": r["fin_res"], "status": r["status"],
+                      "gbs": r["bytes"] / r["seconds"] / 1e9, "block_size": r["block_size"],
+                      "grid_blocks": r["grid_blocks"], "rel_err_vs_tight_fp64": err(x)}
+    speed = {}
+    for kind, mixed, fma, ref in PAIRS:
+        if mixed in out and fma in out:
+            speed[kind] = {"vs_fp64_fma": out[fma]["ms"] / out[mixed]["ms"],
+                           "mixed_over_fp64_iterations":
+                               out[mixed]["inner_iterations"] / max(1, out[fma]["iterations"])}
+            if ref and ref in out:
+                speed[kind]["vs_fp64_reference_arithmetic"] = out[ref]["ms"] / out[mixed]["ms"]
+    out["speedups"] = speed
+    return out
 
 
 def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
@@ -326,6 +419,14 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
     bs = [torch.from_numpy(s.b.copy()).to(dev) for s, _, _ in systems]
     xs = [torch.zeros(s.N, dtype=torch.float64, device=dev) for s, _, _ in systems]
     rows = sum(s.N for s, _, _ in systems)
+    # each system's tight FP64 solution (FP64-FMA, ||r|| <= 1e-12*||b||)
+    tight = pkg.options(precision=pkg.FP64_FMA, tol_mode=pkg.TOL_RELATIVE)
+    x_star, tight_ok = [], 0
+    for (sy, m, p), tp, v, bb in zip(systems, topos, vals, bs):
+        xt = torch.zeros(sy.N, dtype=torch.float64, device=dev)
+        r = tp.solve(v, bb, xt, m, p, 20000, 1e-12, opts=tight, raise_on_error=False)
+        tight_ok += r["status"] == pkg.OK
+        x_star.append(xt)
     variants = {}
     for label, ic in (("ic_exact_bf16", {"ic_bf16": 1}),
                       ("ic_jacobi1_bf16", {"ic_bf16": 1, "ic_sweeps": 1})):
@@ -350,10 +451,13 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
         byts = sum(r["bytes"] for r in res)
+        errs = [float((xk - xs_k).abs().max() / xs_k.abs().max()) for xk, xs_k in zip(xs, x_star)]
         variants[label] = {
             "ms_per_batch": ms, "systems_per_s": count * 1e3 / ms,
             "converged": sum(1 for r in res if r["status"] == pkg.OK),
             "max_iterations": max(r["iterations"] for r in res),
+            "iterations": [r["iterations"] for r in res],
+            "rel_err_vs_tight_fp64": errs, "max_rel_err_vs_tight_fp64": max(errs),
             "gbs": byts / (ms * 1e-3) / 1e9, "tuning": tuning,
             "group_blocks": [r["grid_blocks"] for r in res]}
         plan.close()
@@ -363,8 +467,79 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
                        "pressure, even: BiCG+diag transport, mixed precision, tol 1e-8 relative, "
                        "one graph-captured cooperative launch",
            "variant": best, **variants[best]}
-    out["all_variants"] = {k: {kk: vv for kk, vv in v.items() if kk != "group_blocks"}
+    out["all_variants"] = {k: {kk: vv for kk, vv in v.items()
+                               if kk not in ("group_blocks", "iterations", "rel_err_vs_tight_fp64")}
                            for k, v in variants.items()}
+    out["tight_fp64_converged"] = tight_ok
+    for tp in topos:
+        tp.close()
+    return out
+
+
+def legacy_e2e(pkg, s, method, prec, opts_kw, steps, warmup):
+    """Seconds of `steps` calls of the Fortran-facing C ABI (tflows_cg /
+    _bicg / _cgs) with A, x and b in pinned host memory and the given
+    options set process-wide; host<->device copies are inside each call."""
+    import torch
+    A_h = torch.from_numpy(s.A.copy()).pin_memory().numpy()
+    x_h = torch.zeros(s.NB + s.N + 1, dtype=torch.float64).pin_memory().numpy()
+    r_h = torch.zeros(s.N, dtype=torch.float64).pin_memory().numpy()
+    pkg.set_options(**opts_kw)
+    legacy = {"cg": pkg.cg, "bicg": pkg.bicg, "cgs": pkg.cgs}[method]
+    t = 0.0
+    out = None
+    for k in range(warmup + steps):
+        x_h[:] = 0.0
+        r_h[:] = s.b
+        t0 = time.perf_counter()
+        out = legacy(s.N, s.NB, s.NONZ, A_h, s.Acol, s.Arow, s.Adia, s.Ab, x_h, r_h, prec, 20000,
+                     s.tol)
+        t1 = time.perf_counter()
+        if k >= warmup:
+            t += t1 - t0
+    pkg.set_options()
+    if out.status != pkg.OK:
+        raise RuntimeError(f"e2e solve failed: {out}")
+    return t, {"h2d_bytes_per_step": int(8 * s.nnz + 16 * s.N), "d2h_bytes_per_step": int(16 * s.N)}
+
+
+def cfg2_block(pkg, dev, peak, reps=10, cpu_seconds=10.0):
+    """Config 2: the 128^3 perturbed convection-diffusion system (momentum /
+    scalar transport), BiCG + diagonal in FP64 with fused multiply-adds,
+    device-resident and through tflows_bicg with host buffers, the other
+    config-2 solvers, the GPU answer against the oracle and the one-core
+    oracle throughput."""
+    import numpy as np
+    import torch
+    import oracle
+    s = make_workload(pkg, "cfg2", None)
+    topo = pkg.Topology.from_system(s)
+    val = torch.from_numpy(s.A[:-1].copy()).to(dev)
+    b = torch.from_numpy(s.b.copy()).to(dev)
+    x = torch.zeros(s.N, dtype=torch.float64, device=dev)
+    tuning = topo.autotune(val, b, "bicg", 1, opts=pkg.options(precision=pkg.FP64_FMA))
+    opts = pkg.options(precision=pkg.FP64_FMA, autotune=1)
+    el, res = device_solves(pkg, topo, val, b, x, "bicg", 1, s.tol, opts, reps, 3)
+    kern_s = sum(r["seconds"] for r in res)
+    kern_b = sum(r["bytes"] for r in res)
+    out = {"workload": workload_config(s, "bicg", 1, "fp64_fma")["workload"], "n": s.N,
+           "solves_per_s": reps / el, "ms_per_solve": 1e3 * el / reps,
+           "iterations": res[-1]["iterations"], "launch": tuning,
+           "roofline": {"bound": "hbm", "achieved": kern_b / kern_s / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": kern_b / kern_s / 1e9 / peak,
+                        "kernel": "fma::krylov_kernel<double,0>"}}
+    x_gpu = x.cpu().numpy()
+    t, io = legacy_e2e(pkg, s, "bicg", 1, {"precision": pkg.FP64_FMA, "autotune": 1}, reps, 2)
+    out["e2e"] = {"value": reps / t, "unit": "solves/s", **io}
+    out["methods"] = cfg2_methods(pkg, dev, topo, s, val, b)
+    topo.close()
+    xo, _, it_o, _, _ = oracle.solve("bicg", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
+                                     s.x, s.b, 1, 20000, s.tol)
+    xo = xo[s.NB + 1:]
+    out["rel_err_vs_oracle"] = float(np.abs(x_gpu - xo).max() / np.abs(xo).max())
+    out["oracle_iterations"] = int(it_o)
+    v, n, it, el_c = cpu_reference_throughput(s, "bicg", 1, 1, cpu_seconds)
+    out["cpu_oracle_1core"] = {"solves_per_s": v, "solves": n, "seconds": el_c}
     return out
 
 
@@ -741,35 +916,34 @@ def momentum_block(pkg, dev, n=128, reps=5):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
+    ap.add_argument("--workload", default="cfg3", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
     ap.add_argument("--scale", type=int, default=None, help="box edge (default: the config's)")
-    ap.add_argument("--method", default="bicg")
-    ap.add_argument("--prec", type=int, default=1)
-    ap.add_argument("--precision", default="fp64_fma", choices=["fp64", "fp64_fma", "mixed"],
+    ap.add_argument("--method", default="cg")
+    ap.add_argument("--prec", type=int, default=2)
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "fp64_fma", "mixed"],
                     help="fp64: reference arithmetic; fp64_fma: FP64 with fused multiply-adds "
                          "(within 1e-8 of the reference); mixed: FP32 inner + FP64 refinement")
+    ap.add_argument("--ic-sweeps", type=int, default=0,
+                    help="prec 2: Jacobi sweeps per triangle (0 = exact triangular sweeps)")
+    ap.add_argument("--ic-factors", default="bf16", choices=["bf16", "fp32"],
+                    help="mixed + prec 2: precision of the off-diagonal IC factor entries")
+    ap.add_argument("--oracle-iters", type=int, default=2,
+                    help="CPU legs: whole oracle iterations timed per sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--compare-scale", type=int, default=256,
-                    help="edge of the cfg3 mixed-vs-FP64 comparison (0 = skip)")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-compare", action="store_true", help="skip the config-3 comparison rows")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched (cfg4) block")
-    ap.add_argument("--ic-sweeps", type=int, default=0,
-                    help="mixed + prec 2: Jacobi sweeps per triangle (0 = exact sweeps)")
-    ap.add_argument("--ic-bf16", action="store_true", help="mixed + prec 2: BF16 factor entries")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the config-2 method, config-5 adjoint and SIMPLE-step blocks")
+                    help="skip the config-1/2/5, SIMPLE-step and assembly blocks")
     ap.add_argument("--no-autotune", action="store_true",
                     help="fixed launch shape (256 threads, one slice per warp)")
-    ap.add_argument("--ic-compare-scale", type=int, default=256,
-                    help="edge of the IC mixed-vs-FP64 comparison (0 = skip)")
-    ap.add_argument("--block", default=None, choices=["calcps", "newuvw", "cfg1", "ic"],
+    ap.add_argument("--block", default=None, choices=["calcps", "newuvw", "cfg1", "cfg2", "ic"],
                     help="run only this block (an assembly on a --scale^3 box, default 128, "
-                         "the config-1 latency block, or IC(0) CG on the config-3 system at "
-                         "--scale^3), print its JSON and exit")
+                         "the config-1 latency block, the config-2 block, or IC(0) CG on the "
+                         "config-3 system at --scale^3), print its JSON and exit")
     ap.add_argument("--ic-iters", type=int, default=0,
                     help="--block ic: iteration cap of each solve (0 = to the tolerance)")
     ap.add_argument("--ic-tiled", type=int, default=-1,
@@ -794,6 +968,9 @@ def main():
         if args.block == "cfg1":
             print(json.dumps(cfg1_latency(pkg, dev)), flush=True)
             return
+        if args.block == "cfg2":
+            print(json.dumps(cfg2_block(pkg, dev, load_peaks()[0])), flush=True)
+            return
         if args.block == "ic":
             tiled = (0, 1) if args.ic_tiled < 0 else (args.ic_tiled,)
             print(json.dumps(ic_block(pkg, dev, n=args.scale or 128, iters=args.ic_iters,
@@ -807,7 +984,6 @@ def main():
         print(json.dumps(fn(pkg, dev, n=args.scale or 128)), flush=True)
         return
 
-    import numpy as np
     import torch
     import torch.distributed as dist
 
@@ -822,14 +998,17 @@ def main():
 
     s = make_workload(pkg, args.workload, args.scale)
     method, prec = args.method, args.prec
-    tol = s.tol
     dev = torch.device("cuda", local)
     topo = pkg.Topology.from_system(s)
     val = torch.from_numpy(s.A[:-1].copy()).to(dev)
     b = torch.from_numpy(s.b.copy()).to(dev)
     x = torch.zeros(s.N, dtype=torch.float64, device=dev)
-    prec_mode = {"fp64": pkg.FP64, "fp64_fma": pkg.FP64_FMA, "mixed": pkg.MIXED}[args.precision]
-    ic = {"ic_sweeps": args.ic_sweeps, "ic_bf16": int(args.ic_bf16)}
+    prec_mode = precision_mode(pkg, args.precision)
+    ic = {}
+    if prec == 2:
+        ic["ic_sweeps"] = args.ic_sweeps
+        if args.precision == "mixed" and args.ic_factors == "bf16":
+            ic["ic_bf16"] = 1
     opts = pkg.options(precision=prec_mode, autotune=int(not args.no_autotune), **ic)
     tuning = None
     if not args.no_autotune:
@@ -843,28 +1022,39 @@ def main():
 
     clocks = ClockSampler(local)
     clocks.start()
-    el, results = device_solves(pkg, topo, val, b, x, method, prec, tol, opts, args.steps,
+    el, results = device_solves(pkg, topo, val, b, x, method, prec, s.tol, opts, args.steps,
                                 args.warmup, barrier)
     clk = clocks.stop()
     el = max_over_ranks(el, world, dev)
     value = world * args.steps / el
     kern_s = sum(r["seconds"] for r in results)
     kern_b = sum(r["bytes"] for r in results)
-    iters = [r["iterations"] for r in results]
-
+    last = results[-1]
+    mixed = args.precision == "mixed"
+    dtype = {"fp64": "f64", "fp64_fma": "f64"}.get(args.precision,
+                                                   "f32+bf16+f64" if ic.get("ic_bf16") else "f32+f64")
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64" if args.precision == "mixed" else "f64",
-        "data": "synthetic",
-        "config": workload_config(s, method, prec),
-        "arithmetic": ARITHMETIC[args.precision],
+        "dtype": dtype, "data": "synthetic",
+        "config": workload_config(s, method, prec, args.precision),
+        "arithmetic": ARITHMETIC[args.precision] +
+                      (f"; IC(0) factor entries {args.ic_factors.upper()}, "
+                       + ("exact triangular sweeps" if not args.ic_sweeps
+                          else f"{args.ic_sweeps} Jacobi sweeps per triangle")
+                       if prec == 2 else ""),
         "launch": ({"autotuned": True, **tuning} if tuning else
                    {"autotuned": False, "block_size": 256}),
-        "iterations": int(statistics.median(iters)),
+        "iterations": last["inner_iterations"] if mixed else last["iterations"],
+        "refinements": last["refinements"] if mixed else None,
+        "fin_res": last["fin_res"], "tol": s.tol,
         "time_to_tol_ms": 1e3 * el / args.steps,
     }
+    line["config"]["workload"] = (f"{s.name}: {method} + " +
+                                  ({2: "IC(0)", 1: "diagonal"}.get(prec, "no") + " preconditioning")
+                                  + f", {ARITHMETIC[args.precision]}, to ||r|| < 1e-8*||b|| "
+                                    "(the reference's absolute test), x0 = 0")
     achieved = kern_b / kern_s / 1e9
     kname = {"fp64": "krylov_kernel_fp64", "fp64_fma": "krylov_kernel_fp64_fma",
              "mixed": "mixed_kernel"}[args.precision]
@@ -879,49 +1069,39 @@ def main():
                         "peak_kind": peak_kind}
 
     if not args.no_e2e:
-        # e2e through the Fortran-facing C ABI, inputs in pinned host memory.
-        A_h = torch.from_numpy(s.A.copy()).pin_memory().numpy()
-        x_h = torch.zeros(s.NB + s.N + 1, dtype=torch.float64).pin_memory().numpy()
-        r_h = torch.zeros(s.N, dtype=torch.float64).pin_memory().numpy()
-        pkg.set_options(precision=prec_mode, autotune=int(not args.no_autotune))
-        legacy = {"cg": pkg.cg, "bicg": pkg.bicg, "cgs": pkg.cgs}[method]
-        e2e_t = 0.0
-        for k in range(args.warmup + args.steps):
-            x_h[:] = 0.0
-            r_h[:] = s.b
-            t0 = time.perf_counter()
-            out = legacy(s.N, s.NB, s.NONZ, A_h, s.Acol, s.Arow, s.Adia, s.Ab, x_h, r_h, prec,
-                         20000, tol)
-            t1 = time.perf_counter()
-            if k >= args.warmup:
-                e2e_t += t1 - t0
-        pkg.set_options()
-        if out.status != pkg.OK:
-            raise RuntimeError(f"e2e solve failed: {out}")
-        e2e_t = max_over_ranks(e2e_t, world, dev)
-        line["e2e"] = {"value": world * args.steps / e2e_t, "unit": "solves/s",
-                       "h2d_bytes_per_step": int(8 * s.nnz + 16 * s.N),
-                       "d2h_bytes_per_step": int(16 * s.N)}
-
-    # standalone SELL products (FP64 and FP32) for the SpMV roofline
-    y = torch.empty_like(x)
-    xs = torch.rand(s.N, dtype=torch.float64, device=dev)
-    sl = (s.N + 31) // 32
-    for tag, fp32, sv in (("spmv_fp64", False, 8), ("spmv_fp32", True, 4)):
-        sec = topo.spmv(val, xs, y, repeat=20, fp32=fp32)
-        idx = s.N if topo.patterns else 4.0 * s.nnz  # pattern id per row, or a column per entry
-        byts = s.nnz * sv + idx + 8.0 * (sl + 1) + 2.0 * s.N * sv
-        line[tag] = {"gbs": byts / sec / 1e9, "frac": byts / sec / 1e9 / peak, "us": sec * 1e6,
-                     "bytes": byts}
+        t, io = legacy_e2e(pkg, s, method, prec,
+                           {"precision": prec_mode, "autotune": int(not args.no_autotune), **ic},
+                           args.steps, args.warmup)
+        t = max_over_ranks(t, world, dev)
+        line["e2e"] = {"value": world * args.steps / t, "unit": "solves/s",
+                       "via": f"tflows_{method} (Fortran-facing C ABI), pinned host buffers", **io}
     line["clocks"] = clk
     line["gpu_launches"] = 2 * args.steps
-    x_gpu = x.cpu().numpy()
-    if rank == 0 and not args.no_extras:
-        line["cfg2_methods"] = cfg2_methods(pkg, dev, topo, s, val, b)
+    if rank == 0 and args.workload == "cfg3" and not args.no_compare:
+        headline = {"ms": 1e3 * el / args.steps, "iterations": last["iterations"],
+                    "inner_iterations": last["inner_iterations"],
+                    "refinements": last["refinements"], "fin_res": last["fin_res"],
+                    "status": last["status"], "gbs": achieved,
+                    "block_size": last["block_size"], "grid_blocks": last["grid_blocks"]}
+        line["comparison"] = cfg3_comparison(pkg, dev, topo, s, val, b, headline, x.clone())
+        line["rel_err_vs_tight_fp64"] = line["comparison"]["mixed_ic_exact_bf16"]["rel_err_vs_tight_fp64"]
+        line["speedups"] = line["comparison"]["speedups"]
     topo.close()
-    del val, b, x, y, xs
+    del val, b, x
     torch.cuda.empty_cache()
+    if rank == 0 and not args.no_cpu_baseline:
+        ref_it = (line.get("comparison", {}).get("fp64_ic_exact", {}).get("iterations")
+                  if prec == 2 else None)
+        sampler = OracleSampler(s, method, prec, 1, args.oracle_iters, ref_it)
+        t0 = time.perf_counter()
+        v, _, t_full = sampler.sample()
+        line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
+                                "sample": sampler.describe(time.perf_counter() - t0),
+                                "full_solve_seconds": t_full,
+                                "oracle_full_run_iterations": sampler.full_it}
     if rank == 0 and not args.no_extras:
+        line["cfg2"] = cfg2_block(pkg, dev, peak, cpu_seconds=5.0)
+        torch.cuda.empty_cache()
         line["cfg1_latency"] = cfg1_latency(pkg, dev)
         line["adjoint_cfg5"] = adjoint_cfg5(pkg, dev)
         torch.cuda.empty_cache()
@@ -930,35 +1110,9 @@ def main():
         line["assembly_calcps"] = assembly_block(pkg, dev)
         line["assembly_newuvw"] = momentum_block(pkg, dev)
         torch.cuda.empty_cache()
-
-    if rank == 0 and (args.compare_scale or args.ic_compare_scale):
-        # cfg3 at the comparison scale: diagonal and IC(0) preconditioning
-        same = args.compare_scale == args.ic_compare_scale
-        if args.compare_scale:
-            cmp = mixed_vs_fp64(pkg, dev, args.compare_scale, (1, 2) if same else (1,), 1)
-            line["mixed_vs_fp64"] = cmp[1]
-            if same:
-                line["mixed_vs_fp64_ic"] = cmp[2]
-            torch.cuda.empty_cache()
-        if args.ic_compare_scale and not same:
-            line["mixed_vs_fp64_ic"] = mixed_vs_fp64(pkg, dev, args.ic_compare_scale, (2,), 1)[2]
-            torch.cuda.empty_cache()
     if rank == 0 and not args.no_batch:
         line["batched_cfg4"] = batched_cfg4(pkg, dev, 2, autotune=not args.no_autotune)
         torch.cuda.empty_cache()
-    if rank == 0 and not args.no_cpu_baseline:
-        v, n, it, el_c = cpu_reference_throughput(s, method, prec, 1, args.cpu_seconds)
-        line["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": 1, "kind": "port",
-                                "sample": f"{n} full {method} solves ({it} iterations) of the "
-                                          f"same system, oracle C restatement, 1 thread, "
-                                          f"{el_c:.1f} s"}
-        # the GPU answer against the CPU restatement of the reference
-        import oracle
-        xo, _, it_o, _, _ = oracle.solve(method, s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia,
-                                         s.Ab, s.x, s.b, prec, 20000, tol)
-        xo = xo[s.NB + 1:]
-        line["rel_err_vs_oracle"] = float(np.abs(x_gpu - xo).max() / np.abs(xo).max())
-        line["oracle_iterations"] = int(it_o)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

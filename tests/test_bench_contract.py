@@ -10,8 +10,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_reference_arm_prints_one_json_line():
+    # the config-3 workload at 24^3 (the default 256^3 needs minutes per sample)
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                        "--steps", "1", "--warmup", "3"], capture_output=True, text=True,
+                        "--steps", "1", "--warmup", "3", "--scale", "24"], capture_output=True,
+                       text=True,
                        timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
