@@ -138,6 +138,34 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
+// Explicit shared-memory accesses at 32-bit shared addresses (the tiled
+// sweeps' ring and neighbour exchange): ld.shared / st.shared rather than
+// generic accesses, which the compiler emits when the address space of a
+// pointer carried through structures is not known and which wait on the
+// long scoreboard.  Volatile, so they stay ordered after the barrier waits.
+template <typename T> __device__ __forceinline__ T lds(unsigned a);
+template <> __device__ __forceinline__ double lds<double>(unsigned a) {
+    double v;
+    asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(a));
+    return v;
+}
+template <> __device__ __forceinline__ float lds<float>(unsigned a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+template <> __device__ __forceinline__ unsigned short lds<unsigned short>(unsigned a) {
+    unsigned short v;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ void sts(unsigned a, double v) {
+    asm volatile("st.shared.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+__device__ __forceinline__ void sts(unsigned a, float v) {
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
 // Orders this thread's earlier generic-proxy accesses before its later
 // async-proxy accesses: in shared memory (the block's reads of a ring slot
 // before the bulk copy that refills it; cheap, issued every step) or in

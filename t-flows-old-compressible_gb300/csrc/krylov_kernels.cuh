@@ -783,6 +783,17 @@ __device__ __forceinline__ T tile_coef(const Tiles<T>& tl, const unsigned char* 
     return reinterpret_cast<const T*>(rec + (size_t)f * blockDim.x * sizeof(T))[t];
 }
 
+// The same for a record staged in shared memory, at shared address `rec`.
+template <typename T>
+__device__ __forceinline__ T tile_coef_s(const Tiles<T>& tl, unsigned rec, int f, int t) {
+    if constexpr (sizeof(T) == 4) {
+        if (tl.lu_bf16)
+            return __uint_as_float((unsigned)lds<unsigned short>(rec + (f * blockDim.x + t) * 2u)
+                                   << 16);
+    }
+    return lds<T>(rec + (f * blockDim.x + t) * (unsigned)sizeof(T));
+}
+
 template <typename T>
 __device__ __forceinline__ T& tile_val(const Tiles<T>& tl, unsigned char* rec, int v, int t) {
     return reinterpret_cast<T*>(rec + tile_vfield(tl, v))[t];
@@ -896,8 +907,13 @@ __device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs
     const int B = blockDim.x, t = threadIdx.x, lx = t % kTileX, ly = t / kTileX;
     const int S = tl.steps, ntiles = tl.ntx * tl.nty, H = tl.half;
     const size_t plane = (size_t)S * B;
-    T* nbv = reinterpret_cast<T*>(sm.ring + 2 * H * sm.slot);
-    const unsigned vf0 = tile_vfield(tl, 0), vf1 = tile_vfield(tl, 1), vf2 = tile_vfield(tl, 2);
+    // shared addresses of the ring and of the neighbour exchange (two step
+    // parities of B values); this thread's own offsets within a record
+    const unsigned ring_a = smem_u32(sm.ring);
+    const unsigned nbv_a = ring_a + 2 * H * sm.slot;
+    const unsigned sz = (unsigned)sizeof(T);
+    const unsigned vf0 = tile_vfield(tl, 0) + t * sz, vf1 = tile_vfield(tl, 1) + t * sz,
+                   vf2 = tile_vfield(tl, 2) + t * sz;
     __syncthreads();
     unsigned phase = (unsigned)*sm.phase, pend = 0;
     bool ok = true;
@@ -919,7 +935,7 @@ __device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs
             }
 #pragma unroll
             for (int q = 0; q < 8; ++q)
-                if (s0 + q < S) reinterpret_cast<T*>(recf + (size_t)(s0 + q) * tl.rec_f + vf1)[t] = v[q];
+                if (s0 + q < S) *reinterpret_cast<T*>(recf + (size_t)(s0 + q) * tl.rec_f + vf1) = v[q];
         }
         __syncthreads();
         // edge cells of the left (x-1) and lower (y-1) tiles at step s
@@ -961,39 +977,39 @@ __device__ bool tile_forward(Grid& g, const Mat<T>& m, const T* __restrict__ rhs
             phase ^= 1u << hb;
             pend &= ~(1u << hb);
             const int cnt = min(H, S - s0);
-            const unsigned char* half = sm.ring + (size_t)hb * H * tl.rec_f;
+            const unsigned half = ring_a + (unsigned)(hb * H) * tl.rec_f;
             for (int q = 0; q < cnt; ++q) {
                 const int s = s0 + q;
                 const int z = s - lx - ly;
                 if (inb && z >= 0 && z < tl.nz) {
-                    const unsigned char* sl = half + (size_t)q * tl.rec_f;
-                    const T ri = reinterpret_cast<const T*>(sl + vf1)[t];
+                    const unsigned sl = half + (unsigned)q * tl.rec_f;
+                    const unsigned nb_prev = nbv_a + ((unsigned)((s - 1) & 1) * B + t) * sz;
+                    const T ri = lds<T>(sl + vf1);
                     T acc = ri;
-                    if (z > 0) acc = acc - tile_coef(tl, sl, 0, t) * ycur;
+                    if (z > 0) acc = acc - tile_coef_s(tl, sl, 0, t) * ycur;
                     if (y > 0) {
-                        const T v = ly > 0 ? nbv[((s - 1) & 1) * B + t - kTileX]
+                        const T v = ly > 0 ? lds<T>(nb_prev - kTileX * sz)
                                            : tile_cell(ctl, tmo, sm, ycell + (size_t)s * B,
                                                        (s & 1) ? yp1 : yp0, 27);
-                        acc = acc - tile_coef(tl, sl, 1, t) * v;
+                        acc = acc - tile_coef_s(tl, sl, 1, t) * v;
                     }
                     if (x > 0) {
-                        const T v = lx > 0 ? nbv[((s - 1) & 1) * B + t - 1]
+                        const T v = lx > 0 ? lds<T>(nb_prev - sz)
                                            : tile_cell(ctl, tmo, sm, xcell + (size_t)s * B,
                                                        (s & 1) ? xp1 : xp0, 27);
-                        acc = acc - tile_coef(tl, sl, 2, t) * v;
+                        acc = acc - tile_coef_s(tl, sl, 2, t) * v;
                     }
-                    const T d = reinterpret_cast<const T*>(sl + vf0)[t];
+                    const T d = lds<T>(sl + vf0);
                     const T yv = acc * d;
-                    nbv[(s & 1) * B + t] = yv;
+                    sts(nbv_a + ((unsigned)(s & 1) * B + t) * sz, yv);
                     ycur = yv;
                     const size_t idx = base + (size_t)s * B + t;
                     Cell<T>::store(tl.wt + idx, yv);
                     // the middle step of CG.f90:144-146, for the backward sweep
-                    const T mid = tl.recip ? yv * reinterpret_cast<const T*>(sl + vf2)[t]
-                                           : yv / (d + tiny_v<T>());
+                    const T mid = tl.recip ? yv * lds<T>(sl + vf2) : yv / (d + tiny_v<T>());
                     unsigned char* rb = recb + (size_t)s * tl.rec_b;
-                    reinterpret_cast<T*>(rb + vf1)[t] = mid;
-                    reinterpret_cast<T*>(rb + vf2)[t] = ri;
+                    *reinterpret_cast<T*>(rb + vf1) = mid;
+                    *reinterpret_cast<T*>(rb + vf2) = ri;
                     tl.zt[idx] = Cell<T>::sentinel();
                 }
                 __syncthreads();
@@ -1029,8 +1045,11 @@ __device__ bool tile_backward(Grid& g, const Mat<T>& m, T* __restrict__ zout, Ep
     const int B = blockDim.x, t = threadIdx.x, lx = t % kTileX, ly = t / kTileX;
     const int S = tl.steps, ntiles = tl.ntx * tl.nty, H = tl.half;
     const size_t plane = (size_t)S * B;
-    T* nbv = reinterpret_cast<T*>(sm.ring + 2 * H * sm.slot);
-    const unsigned vf0 = tile_vfield(tl, 0), vf1 = tile_vfield(tl, 1), vf2 = tile_vfield(tl, 2);
+    const unsigned ring_a = smem_u32(sm.ring);
+    const unsigned nbv_a = ring_a + 2 * H * sm.slot;
+    const unsigned sz = (unsigned)sizeof(T);
+    const unsigned vf0 = tile_vfield(tl, 0) + t * sz, vf1 = tile_vfield(tl, 1) + t * sz,
+                   vf2 = tile_vfield(tl, 2) + t * sz;
     __syncthreads();
     unsigned phase = (unsigned)*sm.phase, pend = 0;
     if (t == 0) fence_proxy_async_global();  // the records written before the barrier
@@ -1085,33 +1104,34 @@ __device__ bool tile_backward(Grid& g, const Mat<T>& m, T* __restrict__ zout, Ep
             pend &= ~(1u << hb);
             const int cnt = min(H, S - j0);
             // step S-1-(j0+q) sits at slot H-1-q of the half
-            const unsigned char* half = sm.ring + (size_t)(hb * H + H - 1) * tl.rec_b;
+            const unsigned half = ring_a + (unsigned)(hb * H + H - 1) * tl.rec_b;
             for (int q = 0; q < cnt; ++q) {
                 const int j = j0 + q;
                 const int s = S - 1 - j;
                 const int z = s - lx - ly;
                 if (inb && z >= 0 && z < tl.nz) {
-                    const unsigned char* sl = half - (size_t)q * tl.rec_b;
-                    const T d = reinterpret_cast<const T*>(sl + vf0)[t];
-                    T acc = reinterpret_cast<const T*>(sl + vf1)[t];  // mid
-                    const T ri = reinterpret_cast<const T*>(sl + vf2)[t];
+                    const unsigned sl = half - (unsigned)q * tl.rec_b;
+                    const unsigned nb_prev = nbv_a + ((unsigned)((j - 1) & 1) * B + t) * sz;
+                    const T d = lds<T>(sl + vf0);
+                    T acc = lds<T>(sl + vf1);  // mid
+                    const T ri = lds<T>(sl + vf2);
                     if (x < tl.nx - 1) {
                         const T v = lx < kTileX - 1
-                                        ? nbv[((j - 1) & 1) * B + t + 1]
+                                        ? lds<T>(nb_prev + sz)
                                         : tile_cell(ctl, tmo, sm, xcell + (size_t)s * B,
                                                     (j & 1) ? xp1 : xp0, 29);
-                        acc = acc - tile_coef(tl, sl, 0, t) * v;
+                        acc = acc - tile_coef_s(tl, sl, 0, t) * v;
                     }
                     if (y < tl.ny - 1) {
                         const T v = ly < tl.ty - 1
-                                        ? nbv[((j - 1) & 1) * B + t + kTileX]
+                                        ? lds<T>(nb_prev + kTileX * sz)
                                         : tile_cell(ctl, tmo, sm, ycell + (size_t)s * B,
                                                     (j & 1) ? yp1 : yp0, 29);
-                        acc = acc - tile_coef(tl, sl, 1, t) * v;
+                        acc = acc - tile_coef_s(tl, sl, 1, t) * v;
                     }
-                    if (z < tl.nz - 1) acc = acc - tile_coef(tl, sl, 2, t) * zcur;
+                    if (z < tl.nz - 1) acc = acc - tile_coef_s(tl, sl, 2, t) * zcur;
                     const T zi = acc * d;
-                    nbv[(j & 1) * B + t] = zi;
+                    sts(nbv_a + ((unsigned)(j & 1) * B + t) * sz, zi);
                     zcur = zi;
                     const size_t idx = base + (size_t)s * B + t;
                     Cell<T>::store(tl.zt + idx, zi);
