@@ -62,10 +62,13 @@ typedef struct tflows_options {
                             refinements (default 1e-1)                      */
     int inner_maxiter;   /* mixed, restarted: inner iterations per step     */
     int max_refinements; /* mixed, restarted: refinement steps cap          */
-    int refine_restart;  /* mixed: 1 = restart the inner solve at each FP64
-                            refinement (default, always for CGS); 0 = CG keeps
-                            its search direction across refinements
-                            (reliable updates)                              */
+    int refine_restart;  /* mixed: 0 = reliable updates (default for CG and
+                            BiCG): one FP32 CG stream whose residual is
+                            replaced by the FP64 true residual at each
+                            refinement, keeping the search direction while
+                            the replaced residual had drifted by less than
+                            0.3 of its norm; 1 = restart the inner solve at
+                            each refinement (always for CGS)                */
     int ic_sweeps;       /* prec 2 in mixed or TFLOWS_FP64_FMA solves: 0 =
                             exact triangular sweeps, k > 0 = k Jacobi sweeps
                             per triangle                                    */

@@ -1824,6 +1824,10 @@ static __device__ void mixed_solve(Grid& g, const Mat<double>& m64, const Mat<fl
 }
 
 // ---- mixed precision CG with reliable updates ---------------------------------
+// Drift between the true and the FP32 recursive residual, relative to the
+// latter, above which a reliable update also restarts the search direction.
+constexpr double kReliableDrift = 0.3;
+
 // One FP32 preconditioned CG iteration stream (FP32 values and vectors, FP64
 // reductions).  Whenever its recursive residual has dropped by `inner_rtol`
 // since the last refinement (or below the tolerance), the FP32 correction is
@@ -1869,8 +1873,10 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
     }
     const float* z = prec == 0 ? v.r : v.z;
     // r64 = b - A x; r = (float) r64; xl = 0; ||r||; z = M^-1 r (diag) and (r, z)
-    auto refresh = [&](bool x_zero, double& err, double& rz) -> bool {
-        double a[2] = {0.0, 0.0};
+    // (with `drift`: also ||r_true - r_recursive||^2 into drift, the FP32
+    // recursive residual being the one in v.r before it is replaced)
+    auto refresh = [&](bool x_zero, double& err, double& rz, double* drift) -> bool {
+        double a[3] = {0.0, 0.0, 0.0};
         for (int s = g.wg; s < m64.nslices; s += g.nw) {
             const int i = s * kWarp + g.lane;
             double ri = i < m64.n ? b64[i] : 0.0;
@@ -1878,6 +1884,10 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
             if (i < m64.n) {
                 r64[i] = ri;
                 const float rf = (float)ri;
+                if (drift) {
+                    const double dr = ri - (double)v.r[i];
+                    a[2] += dr * dr;
+                }
                 v.r[i] = rf;
                 v.x[i] = 0.0f;
                 a[0] += ri * ri;
@@ -1890,12 +1900,13 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
                 }
             }
         }
-        publish<2>(g, SLOT_D, a);
+        publish<3>(g, SLOT_D, a);
         if (!grid_sync(g, 82)) return false;
-        double t[2];
-        totals<2>(g, SLOT_D, t);
+        double t[3];
+        totals<3>(g, SLOT_D, t);
         err = sqrt(t[0]);
         rz = t[1];
+        if (drift) *drift = sqrt(t[2]);
         return true;
     };
     auto ic = [&](double& rz) -> bool {
@@ -1911,7 +1922,7 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
         return true;
     };
     double err, rz;
-    if (!refresh(c.x_is_zero != 0, err, rz)) return;
+    if (!refresh(c.x_is_zero != 0, err, rz, nullptr)) return;
     out.ini_res = err;
     out.fin_res = err;
     if (err < tol) {
@@ -1927,12 +1938,13 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
     keep_best();
     double rho = rz, maxr = err, prev = err, best = err;
     int nref = 0, stall = 0, it = 1;
-    bool diverged = false;
+    bool diverged = false, fresh = false;
     const double delta = c.inner_rtol > 0.0 && c.inner_rtol < 1.0 ? c.inner_rtol : 0.1;
     float beta = 0.0f;
     for (; it <= c.maxiter; ++it) {
-        if (it == 1) {
+        if (it == 1 || fresh) {
             TF_FOR4(g, m32, i) { st4(v.p + i, ld4(z + i)); }
+            fresh = false;
         } else {
             TF_FOR4(g, m32, i) {
                 const V4<float> zz = ld4(z + i);
@@ -1998,9 +2010,15 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
                 st4(x64 + i, xd);
             }
             if (!grid_sync(g, 87)) return;
-            if (!refresh(false, err, rz)) return;
+            double drift = 0.0;
+            if (!refresh(false, err, rz, &drift)) return;
             out.fin_res = err;
             out.refinements = ++nref;
+            // Keep the search direction only while the recursive residual
+            // it was built with is still close to the true one; a larger
+            // drift (FP32 recurrences on large, ill-conditioned systems)
+            // restarts it from the new preconditioned residual.
+            fresh = drift > kReliableDrift * rnorm;
             if (err < tol) {
                 out.exit_kind = EXIT_CONVERGED;
                 return;
@@ -2036,12 +2054,12 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
             st4(x64 + i, xd);
         }
         if (!grid_sync(g, 88)) return;
-        if (!refresh(false, err, rz)) return;
+        if (!refresh(false, err, rz, nullptr)) return;
     }
     if (diverged || !(err <= best)) {
         TF_FOR4(g, m64, i) { st4(x64 + i, ld4(xbest + i)); }
         if (!grid_sync(g, 89)) return;
-        if (!refresh(false, err, rz)) return;
+        if (!refresh(false, err, rz, nullptr)) return;
     }
     out.fin_res = err;
     out.exit_kind = err < tol ? EXIT_CONVERGED : EXIT_MAXITER;

@@ -69,7 +69,7 @@ void default_opts(tflows_options* o) {
     o->precision = TFLOWS_FP64;
     o->tol_mode = TFLOWS_TOL_ABSOLUTE;
     o->inner_rtol = 1e-1;
-    o->refine_restart = 1;
+    o->refine_restart = 0;
     o->inner_maxiter = 2000;
     o->max_refinements = 30;
     o->ic_sweeps = 0;
