@@ -40,14 +40,33 @@ def test_launch_shapes_give_the_same_answer(method, prec, precision, block, rpw)
     else:
         s = mesh.convection_diffusion_system(20, 18, 16, perturb=0.2, seed=5)
     topo = tflows.Topology.from_system(s)
-    x0, r0 = _solve(topo, s, method, prec, precision=precision)
+    # mixed: restarted refinement, whose iterates depend on the launch shape
+    # only through rounding (reliable updates decide on direction restarts
+    # by a threshold that rounding can flip; see the test below)
+    kw = {"refine_restart": 1} if precision == 1 else {}
+    x0, r0 = _solve(topo, s, method, prec, precision=precision, **kw)
     x1, r1 = _solve(topo, s, method, prec, precision=precision, block_size=block,
-                    rows_per_warp=rpw, sweep_warps=2)
+                    rows_per_warp=rpw, sweep_warps=2, **kw)
     assert r0["status"] == r1["status"] == tflows.OK, (r0, r1)
     assert r1["block_size"] == block
     assert abs(r0["iterations"] - r1["iterations"]) <= 1, (r0, r1)
     tol = 1e-8 if precision == 0 else 1e-7
     assert np.abs(x1 - x0).max() <= tol * np.abs(x0).max()
+    topo.close()
+
+
+@pytest.mark.parametrize("block,rpw", [(128, 0), (512, 0), (256, 256)])
+def test_reliable_updates_across_launch_shapes(block, rpw):
+    """Mixed CG with reliable updates (the default refinement): every launch
+    shape reaches the tolerance with a solution within the refinement
+    accuracy of the default shape's, and within 25 % of its iterations."""
+    s = mesh.pressure_system(20, 18, 16, perturb=0.2, seed=11, variable_density=True)
+    topo = tflows.Topology.from_system(s)
+    x0, r0 = _solve(topo, s, "cg", 2, precision=1)
+    x1, r1 = _solve(topo, s, "cg", 2, precision=1, block_size=block, rows_per_warp=rpw)
+    assert r0["status"] == r1["status"] == tflows.OK, (r0, r1)
+    assert abs(r0["iterations"] - r1["iterations"]) <= max(2, r0["iterations"] // 4), (r0, r1)
+    assert np.abs(x1 - x0).max() <= 1e-7 * np.abs(x0).max()
     topo.close()
 
 
