@@ -205,7 +205,12 @@ __global__ void __launch_bounds__(kMaxBlock, kMinBlocksAtMax)
         out.ini_res = 0.0;
         out.fin_res = 0.0;
         out.bnrm2 = 0.0;
-        mixed_solve(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.v32, P.cfg, out);
+        // the refinement the system asked for, as in its single-system solve
+        if (it.method != 2 && !P.cfg.restart)
+            mixed_cg_reliable(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.xbest, P.v32, P.cfg,
+                              out);
+        else
+            mixed_solve(g, P.m64, P.m32, P.x64, P.r64, P.b64, P.D64, P.v32, P.cfg, out);
         if (g.bid == 0 && threadIdx.x == 0) {
             DevState* s = P.state;
             SolveOut o;
