@@ -635,11 +635,11 @@ double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevSta
     if (rq.precision == 1) {
         const double spmv32 = (double)t.nnz * 8.0 + sl + 8.0 * t.n;
         const double ic = rq.prec == 2 ? ic_bytes(rq.ic_bf16 ? 2.0 : 4.0, 4.0) : 0.0;
-        // restarted CG forms its search direction inside the product (z and
-        // p read once, p and q written once), so
-        // the product's own vector read and write are part of the 4·N·12
-        // (resp. 10) vector bytes
-        const double cg_fused = !rq.refine_restart ? 8.0 * t.n : 0.0;
+        // the inner CG (restarted or with reliable updates) forms its search
+        // direction inside the product (z and p read once, p and q written
+        // once), so the product's own vector read and write are part of the
+        // 4·N·12 (resp. 10) vector bytes
+        const double cg_fused = 0.0;
         const double inner_it = cgs ? 2 * spmv32 + 4.0 * t.n * 22 + 2 * ic
                                     : spmv32 - 8.0 * t.n + cg_fused +
                                           4.0 * t.n * (rq.prec == 1 ? 12 : 10) + ic;
@@ -647,8 +647,10 @@ double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevSta
     }
     const int it = std::max(0, std::min(st.iterations, rq.maxiter));
     const double ic = rq.prec == 2 ? ic_bytes(8.0, 8.0) : 0.0;
+    // CG forms its next search direction inside the product: z and the old
+    // p read, the new p and q written there, no separate update pass
     const double per_it = cgs ? 2 * spmv64 + 8.0 * t.n * 22 + 2 * ic
-                              : spmv64 + 8.0 * t.n * (rq.prec == 1 ? 12 : 10) + ic;
+                              : spmv64 + 8.0 * t.n * ((rq.prec == 1 ? 12 : 10) - 1) + ic;
     return per_it * it + spmv64 + 8.0 * t.n * 4;
 }
 

@@ -331,6 +331,48 @@ __device__ __forceinline__ T sell_row(const Mat<T>& m, int s, int lane, const X*
 __device__ __forceinline__ float fused_dir(float z, float beta, float p, bool first) {
     return first ? z : __fmaf_rn(beta, p, z);
 }
+// FP64: z + beta p written as the separate update pass writes it, so each
+// build (contracted or not) forms the same value either way.
+__device__ __forceinline__ double fused_dir(double z, double beta, double p, bool first) {
+    return first ? z : z + beta * p;
+}
+
+// The FP64 product with the next search direction formed in the gather
+// (column patterns where the topology has them, plain left-to-right sums as
+// the reference's product): the same direction and the same q as the
+// separate update pass followed by the product, bit for bit, with one vector
+// pass and one grid barrier less per iteration.
+__device__ __forceinline__ double sell_row_dir(const Mat<double>& m, int s, int lane,
+                                               const double* __restrict__ z,
+                                               const double* __restrict__ p, double beta,
+                                               bool first) {
+    const long long b0 = m.soff[s];
+    const int w = (int)((m.soff[s + 1] - b0) >> 5);
+    const int* cp = m.scol + b0 + lane;
+    const double* vp = m.sval + b0 + lane;
+    double acc = 0.0;
+    if (w <= 8) {
+        int c[8];
+        double v[8], zz[8], pp[8];
+        sell_cols8(m, s, lane, w, b0, c);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) v[t] = t < w ? vp[32 * t] : 0.0;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            zz[t] = c[t] >= 0 ? z[c[t]] : 0.0;
+            pp[t] = c[t] >= 0 && !first ? p[c[t]] : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (c[t] >= 0) acc = acc + v[t] * fused_dir(zz[t], beta, pp[t], first);
+        return acc;
+    }
+    for (int t = 0; t < w; ++t) {
+        const int c = cp[32 * t];
+        if (c >= 0) acc = acc + vp[32 * t] * fused_dir(z[c], beta, first ? 0.0 : p[c], first);
+    }
+    return acc;
+}
 
 __device__ __forceinline__ float sell_row_dir(const Mat<float>& m, int s, int lane,
                                               const float* __restrict__ z,
@@ -1260,7 +1302,7 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
     double rho = 0.0, rhoold = 0.0;
     bool nonfinite = false;
     int iter = 1;
-    // search direction; the FP32 inner solves alternate between p and t
+    // search direction: alternates between p and t (formed in the product)
     T* pcur = v.p;
     T* pnext = v.t;
     for (; iter <= cfg.maxiter; ++iter) {
@@ -1277,61 +1319,29 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         } else {
             rho = rho_next;
         }
-        bool fused = false;
-        if constexpr (sizeof(T) == 4) {
-            {
-                // FP32 inner solves: the new search direction goes into the
-                // other p buffer as the product forms it (no separate update
-                // pass, one barrier less per iteration)
-                const float beta = iter == 1 ? 0.f : float(rho / rhoold);
-                const bool first = iter == 1;
-                const float* pold = pcur;
-                float* pnew = pnext;
-                float a1[1] = {0.f};
-                for (int s = g.wg; s < m.nslices; s += g.nw) {
-                    const int i = s * kWarp + g.lane;
-                    const float qi = sell_row_dir(m, s, g.lane, z, pold, beta, first);
-                    if (i < m.n) {
-                        const float pi = fused_dir(z[i], beta, first ? 0.f : pold[i], first);
-                        pnew[i] = pi;
-                        v.q[i] = qi;
-                        a1[0] += pi * qi;
-                    }
+        {
+            // the new search direction goes into the other p buffer as the
+            // product forms it (no separate update pass, one barrier less per
+            // iteration)
+            const T beta = iter == 1 ? T(0) : T(rho / rhoold);
+            const bool first = iter == 1;
+            const T* pold = pcur;
+            T* pnew = pnext;
+            T a1[1] = {T(0)};
+            for (int s = g.wg; s < m.nslices; s += g.nw) {
+                const int i = s * kWarp + g.lane;
+                const T qi = sell_row_dir(m, s, g.lane, z, pold, beta, first);
+                if (i < m.n) {
+                    const T pi = fused_dir(z[i], beta, first ? T(0) : pold[i], first);
+                    pnew[i] = pi;
+                    v.q[i] = qi;
+                    a1[0] += pi * qi;
                 }
-                pcur = pnew;
-                pnext = const_cast<float*>(pold);
-                publish_t<1>(g, SLOT_C, a1);
-                if (!grid_sync(g, 43)) { out.exit_kind = EXIT_ABORT; return; }
-                fused = true;
             }
-        }
-        if (!fused) {
-        // p = z + beta p  (CG.f90:178-187)
-        if (iter == 1) {
-            TF_FOR4(g, m, i) { st4(v.p + i, ld4(z + i)); }
-        } else {
-            const T beta = T(rho / rhoold);
-            TF_FOR4(g, m, i) {
-                const V4<T> zz = ld4(z + i);
-                V4<T> pp = ld4(v.p + i);
-#pragma unroll
-                for (int u = 0; u < 4; ++u) pp.a[u] = zz.a[u] + beta * pp.a[u];
-                st4(v.p + i, pp);
-            }
-        }
-        if (!grid_sync(g, 42)) { out.exit_kind = EXIT_ABORT; return; }
-        // q = A p; (p, q)  (CG.f90:193-218)
-        T a1[1] = {T(0)};
-        for (int s = g.wg; s < m.nslices; s += g.nw) {
-            const int i = s * kWarp + g.lane;
-            const T qi = sell_row(m, s, g.lane, v.p);
-            if (i < m.n) {
-                v.q[i] = qi;
-                a1[0] += v.p[i] * qi;
-            }
-        }
-        publish_t<1>(g, SLOT_C, a1);
-        if (!grid_sync(g, 43)) { out.exit_kind = EXIT_ABORT; return; }
+            pcur = pnew;
+            pnext = const_cast<T*>(pold);
+            publish_t<1>(g, SLOT_C, a1);
+            if (!grid_sync(g, 43)) { out.exit_kind = EXIT_ABORT; return; }
         }
         double t1[1];
         totals<1>(g, SLOT_C, t1);
@@ -1939,40 +1949,41 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
     double rho = rz, maxr = err, prev = err, best = err;
     int nref = 0, stall = 0, it = 1;
     bool diverged = false, fresh = false;
+    float* pcur = v.p;  // search direction: alternates between p and t
+    float* pnext = v.t;
     const double delta = c.inner_rtol > 0.0 && c.inner_rtol < 1.0 ? c.inner_rtol : 0.1;
     float beta = 0.0f;
     for (; it <= c.maxiter; ++it) {
-        if (it == 1 || fresh) {
-            TF_FOR4(g, m32, i) { st4(v.p + i, ld4(z + i)); }
+        {
+            // next search direction formed inside the product (p = z on the
+            // first iteration and after a restart), into the other buffer
+            const bool first = it == 1 || fresh;
             fresh = false;
-        } else {
-            TF_FOR4(g, m32, i) {
-                const V4<float> zz = ld4(z + i);
-                V4<float> pp = ld4(v.p + i);
-#pragma unroll
-                for (int u = 0; u < 4; ++u) pp.a[u] = zz.a[u] + beta * pp.a[u];
-                st4(v.p + i, pp);
+            const float* pold = pcur;
+            float* pnew = pnext;
+            float a1[1] = {0.f};
+            for (int s = g.wg; s < m32.nslices; s += g.nw) {
+                const int i = s * kWarp + g.lane;
+                const float qi = sell_row_dir(m32, s, g.lane, z, pold, beta, first);
+                if (i < m32.n) {
+                    const float pi = fused_dir(z[i], beta, first ? 0.f : pold[i], first);
+                    pnew[i] = pi;
+                    v.q[i] = qi;
+                    a1[0] += pi * qi;
+                }
             }
+            pcur = pnew;
+            pnext = const_cast<float*>(pold);
+            publish_t<1>(g, SLOT_C, a1);
+            if (!grid_sync(g, 85)) return;
         }
-        if (!grid_sync(g, 84)) return;
-        float a1[1] = {0.f};
-        for (int s = g.wg; s < m32.nslices; s += g.nw) {
-            const int i = s * kWarp + g.lane;
-            const float qi = sell_row(m32, s, g.lane, v.p);
-            if (i < m32.n) {
-                v.q[i] = qi;
-                a1[0] += v.p[i] * qi;
-            }
-        }
-        publish_t<1>(g, SLOT_C, a1);
-        if (!grid_sync(g, 85)) return;
         double t1[1];
         totals<1>(g, SLOT_C, t1);
         const float alfa = (float)(rho / t1[0]);
         float a3[2] = {0.f, 0.f};
         TF_FOR4(g, m32, i) {
             V4<float> xx = ld4(v.x + i), rr = ld4(v.r + i), zz;
-            const V4<float> pp = ld4(v.p + i), qq = ld4(v.q + i);
+            const V4<float> pp = ld4(pcur + i), qq = ld4(v.q + i);
             V4<float> dd;
             if (prec == 1) dd = ld4(v.D + i);
 #pragma unroll
