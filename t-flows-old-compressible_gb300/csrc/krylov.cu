@@ -422,6 +422,13 @@ bool tiles_env_on() {
 
 size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
+// FP64 CG forms its search direction inside the product only on systems
+// whose vectors stay in L2 (measured: config 1, 32^3, 18.0 -> 16.7 us per
+// iteration; on 128^3 and 256^3 it was 20-30 % slower, the second gathered
+// vector and the per-neighbour z + beta p on the FP64 pipe costing more than
+// the update pass it saves).
+bool fuse_dir_fp64(const DeviceTopology& t) { return t.n <= (1 << 19); }
+
 struct TileGeom {
     int ty = 0, ntx = 0, nty = 0, steps = 0;
     long long slots = 0;
@@ -554,6 +561,7 @@ cudaError_t prepare_fp64(const DeviceTopology& t, Workspace& ws, const SolveRequ
     P.mode = 0;
     P.stall = rq.inject_stall;
     P.cfg.ic_sweeps = rq.prec == 2 ? std::max(rq.ic_sweeps, 0) : 0;
+    P.cfg.fuse_dir = fuse_dir_fp64(t) ? 1 : 0;
     cudaError_t e = cudaMemsetAsync(ws.ctl, 0, sizeof(DevCtl), s);
     if (rq.prec == 2) {
         const long long nvec = (long long)t.nslices * kWarp;
@@ -635,11 +643,11 @@ double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevSta
     if (rq.precision == 1) {
         const double spmv32 = (double)t.nnz * 8.0 + sl + 8.0 * t.n;
         const double ic = rq.prec == 2 ? ic_bytes(rq.ic_bf16 ? 2.0 : 4.0, 4.0) : 0.0;
-        // the inner CG (restarted or with reliable updates) forms its search
-        // direction inside the product (z and p read once, p and q written
-        // once), so the product's own vector read and write are part of the
-        // 4·N·12 (resp. 10) vector bytes
-        const double cg_fused = 0.0;
+        // restarted CG forms its search direction inside the product (z and
+        // p read once, p and q written once), so the product's own vector
+        // read and write are part of the 4·N·12 (resp. 10) vector bytes; the
+        // reliable-update loop keeps its separate direction pass
+        const double cg_fused = !rq.refine_restart ? 8.0 * t.n : 0.0;
         const double inner_it = cgs ? 2 * spmv32 + 4.0 * t.n * 22 + 2 * ic
                                     : spmv32 - 8.0 * t.n + cg_fused +
                                           4.0 * t.n * (rq.prec == 1 ? 12 : 10) + ic;
@@ -647,10 +655,12 @@ double solve_bytes(const DeviceTopology& t, const SolveRequest& rq, const DevSta
     }
     const int it = std::max(0, std::min(st.iterations, rq.maxiter));
     const double ic = rq.prec == 2 ? ic_bytes(8.0, 8.0) : 0.0;
-    // CG forms its next search direction inside the product: z and the old
-    // p read, the new p and q written there, no separate update pass
+    // CG on a small system forms its next search direction inside the
+    // product (z and the old p read, the new p and q written there, no
+    // separate update pass: one vector fewer)
     const double per_it = cgs ? 2 * spmv64 + 8.0 * t.n * 22 + 2 * ic
-                              : spmv64 + 8.0 * t.n * ((rq.prec == 1 ? 12 : 10) - 1) + ic;
+                              : spmv64 + 8.0 * t.n * ((rq.prec == 1 ? 12 : 10) -
+                                                      (fuse_dir_fp64(t) ? 1 : 0)) + ic;
     return per_it * it + spmv64 + 8.0 * t.n * 4;
 }
 

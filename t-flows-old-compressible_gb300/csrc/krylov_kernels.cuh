@@ -158,6 +158,7 @@ struct SolveCfg {
     int do_prec1;   // compute D (Prec1) in this launch
     int tol_is_relative;  // tol multiplies ||b||
     int ic_sweeps;  // prec 2: 0 = exact triangular sweeps, k > 0 = k Jacobi sweeps each
+    int fuse_dir;   // FP64 CG: form the search direction inside the product
 };
 
 struct SolveOut {
@@ -373,6 +374,7 @@ __device__ __forceinline__ double sell_row_dir(const Mat<double>& m, int s, int 
     }
     return acc;
 }
+
 
 __device__ __forceinline__ float sell_row_dir(const Mat<float>& m, int s, int lane,
                                               const float* __restrict__ z,
@@ -1302,7 +1304,7 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
     double rho = 0.0, rhoold = 0.0;
     bool nonfinite = false;
     int iter = 1;
-    // search direction: alternates between p and t (formed in the product)
+    // search direction; the FP32 inner solves alternate between p and t
     T* pcur = v.p;
     T* pnext = v.t;
     for (; iter <= cfg.maxiter; ++iter) {
@@ -1319,10 +1321,14 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
         } else {
             rho = rho_next;
         }
-        {
-            // the new search direction goes into the other p buffer as the
-            // product forms it (no separate update pass, one barrier less per
-            // iteration)
+        // The new search direction formed inside the product, into the other
+        // p buffer (no separate update pass, one barrier less per
+        // iteration): always in the FP32 inner solves; in FP64 where the
+        // host asked for it (systems whose vectors stay in L2 -- on larger
+        // ones gathering z and p and forming z + beta p per neighbour on the
+        // FP64 pipe costs more than the pass it saves).
+        const bool fused = sizeof(T) == 4 || cfg.fuse_dir;
+        if (fused) {
             const T beta = iter == 1 ? T(0) : T(rho / rhoold);
             const bool first = iter == 1;
             const T* pold = pcur;
@@ -1342,6 +1348,34 @@ __device__ void cg_solve(Grid& g, const Mat<T>& m, Vecs<T>& v, const SolveCfg& c
             pnext = const_cast<T*>(pold);
             publish_t<1>(g, SLOT_C, a1);
             if (!grid_sync(g, 43)) { out.exit_kind = EXIT_ABORT; return; }
+        }
+        if (!fused) {
+        // p = z + beta p  (CG.f90:178-187)
+        if (iter == 1) {
+            TF_FOR4(g, m, i) { st4(v.p + i, ld4(z + i)); }
+        } else {
+            const T beta = T(rho / rhoold);
+            TF_FOR4(g, m, i) {
+                const V4<T> zz = ld4(z + i);
+                V4<T> pp = ld4(v.p + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) pp.a[u] = zz.a[u] + beta * pp.a[u];
+                st4(v.p + i, pp);
+            }
+        }
+        if (!grid_sync(g, 42)) { out.exit_kind = EXIT_ABORT; return; }
+        // q = A p; (p, q)  (CG.f90:193-218)
+        T a1[1] = {T(0)};
+        for (int s = g.wg; s < m.nslices; s += g.nw) {
+            const int i = s * kWarp + g.lane;
+            const T qi = sell_row(m, s, g.lane, v.p);
+            if (i < m.n) {
+                v.q[i] = qi;
+                a1[0] += v.p[i] * qi;
+            }
+        }
+        publish_t<1>(g, SLOT_C, a1);
+        if (!grid_sync(g, 43)) { out.exit_kind = EXIT_ABORT; return; }
         }
         double t1[1];
         totals<1>(g, SLOT_C, t1);
@@ -1949,41 +1983,40 @@ static __device__ void mixed_cg_reliable(Grid& g, const Mat<double>& m64, const 
     double rho = rz, maxr = err, prev = err, best = err;
     int nref = 0, stall = 0, it = 1;
     bool diverged = false, fresh = false;
-    float* pcur = v.p;  // search direction: alternates between p and t
-    float* pnext = v.t;
     const double delta = c.inner_rtol > 0.0 && c.inner_rtol < 1.0 ? c.inner_rtol : 0.1;
     float beta = 0.0f;
     for (; it <= c.maxiter; ++it) {
-        {
-            // next search direction formed inside the product (p = z on the
-            // first iteration and after a restart), into the other buffer
-            const bool first = it == 1 || fresh;
+        if (it == 1 || fresh) {
+            TF_FOR4(g, m32, i) { st4(v.p + i, ld4(z + i)); }
             fresh = false;
-            const float* pold = pcur;
-            float* pnew = pnext;
-            float a1[1] = {0.f};
-            for (int s = g.wg; s < m32.nslices; s += g.nw) {
-                const int i = s * kWarp + g.lane;
-                const float qi = sell_row_dir(m32, s, g.lane, z, pold, beta, first);
-                if (i < m32.n) {
-                    const float pi = fused_dir(z[i], beta, first ? 0.f : pold[i], first);
-                    pnew[i] = pi;
-                    v.q[i] = qi;
-                    a1[0] += pi * qi;
-                }
+        } else {
+            TF_FOR4(g, m32, i) {
+                const V4<float> zz = ld4(z + i);
+                V4<float> pp = ld4(v.p + i);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) pp.a[u] = zz.a[u] + beta * pp.a[u];
+                st4(v.p + i, pp);
             }
-            pcur = pnew;
-            pnext = const_cast<float*>(pold);
-            publish_t<1>(g, SLOT_C, a1);
-            if (!grid_sync(g, 85)) return;
         }
+        if (!grid_sync(g, 84)) return;
+        float a1[1] = {0.f};
+        for (int s = g.wg; s < m32.nslices; s += g.nw) {
+            const int i = s * kWarp + g.lane;
+            const float qi = sell_row(m32, s, g.lane, v.p);
+            if (i < m32.n) {
+                v.q[i] = qi;
+                a1[0] += v.p[i] * qi;
+            }
+        }
+        publish_t<1>(g, SLOT_C, a1);
+        if (!grid_sync(g, 85)) return;
         double t1[1];
         totals<1>(g, SLOT_C, t1);
         const float alfa = (float)(rho / t1[0]);
         float a3[2] = {0.f, 0.f};
         TF_FOR4(g, m32, i) {
             V4<float> xx = ld4(v.x + i), rr = ld4(v.r + i), zz;
-            const V4<float> pp = ld4(pcur + i), qq = ld4(v.q + i);
+            const V4<float> pp = ld4(v.p + i), qq = ld4(v.q + i);
             V4<float> dd;
             if (prec == 1) dd = ld4(v.D + i);
 #pragma unroll
