@@ -8,6 +8,7 @@ iterates agree to rounding) and reach each system's tolerance.
 import numpy as np
 import pytest
 
+import oracle
 from conftest import tflows
 
 mesh = tflows.mesh
@@ -109,7 +110,7 @@ def test_simple_step_plan_on_one_topology(precision):
     """The five solves of one SIMPLE outer iteration -- mixture fraction (cg),
     three momentum components (bicg) and pressure correction (cg, IC) -- on
     one mesh topology, replayed from one captured plan; each system must
-    match its own single-system solve."""
+    match its own single-system solve and the oracle's solve."""
     import torch
     cd = mesh.convection_diffusion_system(14, 12, 10, perturb=0.2, seed=21)
     zm = mesh.convection_diffusion_system(14, 12, 10, perturb=0.2, seed=22)
@@ -126,6 +127,13 @@ def test_simple_step_plan_on_one_topology(precision):
     tols = [1e-10 * float(np.linalg.norm(b)) for b in rhs]
     opts = tflows.options(precision=precision)
     plan = tflows.Plan([topo] * 5, vals, bs, xs, methods, precs, [3000] * 5, tols, opts)
+    # each system's oracle solve (Process/CG.f90, BiCG.f90 restated), 1000x tighter
+    xo = []
+    for k in range(5):
+        m = mats[k]
+        xk, *_ = oracle.solve(methods[k], m.N, m.NB, m.NONZ, m.A, m.Acol, m.Arow, m.Adia, m.Ab,
+                              m.x, rhs[k], precs[k], 20000, 1e-3 * tols[k])
+        xo.append(xk[m.NB + 1:])
     for _ in range(2):
         for x in xs:
             x.zero_()
@@ -140,5 +148,6 @@ def test_simple_step_plan_on_one_topology(precision):
             xa, xb = xs[k].cpu().numpy(), x1.cpu().numpy()
             assert np.abs(xa - xb).max() <= 1e-7 * np.abs(xb).max(), k
             assert np.linalg.norm(rhs[k] - mats[k].scipy() @ xa) < 2 * tols[k]
+            assert np.abs(xa - xo[k]).max() <= 1e-6 * np.abs(xo[k]).max(), k
     plan.close()
     topo.close()
