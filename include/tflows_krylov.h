@@ -35,6 +35,8 @@ extern "C" {
 #define TFLOWS_CUDA_ERROR     6 /* a CUDA runtime call failed              */
 #define TFLOWS_NO_DEVICE      7 /* no CUDA device available                */
 #define TFLOWS_UNSUPPORTED    8 /* option combination not implemented      */
+#define TFLOWS_HALO_ERROR     9 /* a halo exchange or global-sum callback
+                                   returned nonzero (tflows_set_halo)      */
 
 /* ---- methods, precisions, tolerance modes -------------------------------- */
 #define TFLOWS_METHOD_CG        0 /* Process/CG.f90                          */
@@ -178,6 +180,43 @@ const char *tflows_last_error(void);
 void tflows_last_result(tflows_result *res);
 /* Release every device resource the library holds. */
 void tflows_finalize(void);
+
+/* ---- subdomain coupling: halo maps and rank callbacks -------------------- */
+/* A run split into subdomains, one per rank (T-FlowS with Npro > 0), couples
+ * its rows to buffer cells k = -NB..-1 of x(-NB:N) whose values live on the
+ * neighbouring ranks.  Without a registered halo, Ab is not read: the
+ * reference's one-domain run (Npro = 0), where the subdomain loops are
+ * empty.  With one, the legacy entry points (and tflows_solve_ex with
+ * TFLOWS_FP64; other precisions return TFLOWS_UNSUPPORTED) run the
+ * reference's coupled algorithm on the device in reference arithmetic:
+ *   - after every product q = A p the buffer cells of p are exchanged and
+ *     q(BufInd(k)) += Ab(k) p(k) is added (Process/CG.f90:200-208,
+ *     BiCG.f90:202-211, CGS.f90:201-208 and :301-308);
+ *   - every inner product and norm is summed over the ranks (glosum);
+ *   - tflows_resid subtracts Ab(k) x(k) with the caller's x(-NB:-1)
+ *     (Resid.f90:36-42; no exchange, as the reference).
+ * The transport stays with the caller, through two callbacks:
+ *   exchange(user, phi, NB): phi points at PHI(-NB) of a host copy whose
+ *     buffer cells already hold the values of the cells they mirror,
+ *     PHI(c) = PHI(BufInd(c)) (Parallel/Double/Exchng.f90:36-43); swap each
+ *     neighbour's segment PHI(NBBe(sub):NBBs(sub)) with rank sub-1 in place,
+ *     as MPI_SENDRECV_REPLACE does (Exchng.f90:46-60);
+ *   glosum(user, value): replace *value by its sum over the ranks
+ *     (Parallel/Double/GloSum.f90, MPI_ALLREDUCE).
+ * Both return 0 on success; anything else ends the call with
+ * TFLOWS_HALO_ERROR.  Every rank makes the same solver calls: the number of
+ * exchanges and sums per call is the same on all ranks.
+ * Maps as par_mod holds them after Parallel/Double/BufLoa.f90:35-84:
+ * NBBs[sub-1] = NBBs(sub), NBBe[sub-1] = NBBe(sub) for sub = 1..Npro (a
+ * neighbour without connections has NBBe(sub) > NBBs(sub)); BufInd passed
+ * from BufInd(-NB), so BufInd[NB + k] = BufInd(k) in 1..N for every buffer
+ * cell k.  NB must equal the NB of the solver calls.  The registration is
+ * process-wide, as par_mod is; Npro = 0 or tflows_clear_halo removes it. */
+typedef int (*tflows_exchange_fn)(void *user, double *phi, int NB);
+typedef int (*tflows_glosum_fn)(void *user, double *value);
+int tflows_set_halo(int Npro, int NB, const int *NBBs, const int *NBBe, const int *BufInd,
+                    tflows_exchange_fn exchange, tflows_glosum_fn glosum, void *user);
+void tflows_clear_halo(void);
 
 /* ---- extended host-pointer entry point ------------------------------------ */
 /* Same arguments and outputs as tflows_cg/bicg/cgs plus a method, options

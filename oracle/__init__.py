@@ -21,6 +21,8 @@ _lock = threading.Lock()
 
 _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int)
+EXCHANGE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, _D, ctypes.c_int)
+GLOSUM_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, _D)
 
 
 def build(force: bool = False) -> str:
@@ -51,6 +53,13 @@ def lib():
             L.oracle_resid.restype = None
             L.oracle_topolm.argtypes = [ctypes.c_int, ctypes.c_int, _I, _I, _I, _I, _I]
             L.oracle_topolm.restype = ctypes.c_int
+            L.oracle_set_halo.argtypes = [ctypes.c_int, ctypes.c_int, _I, _I, _I, EXCHANGE_FN,
+                                          GLOSUM_FN, ctypes.c_void_p]
+            L.oracle_set_halo.restype = None
+            L.oracle_clear_halo.argtypes = []
+            L.oracle_clear_halo.restype = None
+            L.oracle_halo_failed.argtypes = []
+            L.oracle_halo_failed.restype = ctypes.c_int
             L.oracle_reset_state.argtypes = []
             L.oracle_reset_state.restype = None
             L.oracle_error_state.argtypes = []
@@ -106,6 +115,48 @@ def solve(method, N, NB, NONZ, A, Acol, Arow, Adia, Ab, x, r1, prec, niter, tol,
     fn(int(N), int(NB), int(NONZ), _dp(A), _ip(Acol), _ip(Arow), _ip(Adia), _dp(Ab), _dp(xo),
        _dp(ro), int(prec), ctypes.byref(it), float(tol), ctypes.byref(ini), ctypes.byref(fin))
     return xo, ro, it.value, ini.value, fin.value
+
+
+class halo:
+    """Context manager: the oracle's subdomain run on the calling thread
+    (oracle_set_halo).  ``NBBs``/``NBBe``: NBBs(sub), NBBe(sub) for
+    sub = 1..Npro; ``BufInd``: BufInd(-NB:-1).  ``exchange(phi)`` swaps the
+    neighbours' segments of PHI(-NB:-1) (``phi[NB + k]`` = PHI(k)) in place;
+    ``glosum(v)`` returns the sum of ``v`` over the ranks.  Raises on exit
+    when a callback failed."""
+
+    def __init__(self, Npro, NB, NBBs, NBBe, BufInd, exchange, glosum):
+        self.args = (_i32(NBBs), _i32(NBBe), _i32(BufInd if NB > 0 else np.zeros(1)))
+        self.Npro, self.NB = int(Npro), int(NB)
+
+        def _ex(user, phi, nb):
+            try:
+                exchange(np.ctypeslib.as_array(phi, shape=(nb,)))
+                return 0
+            except Exception:
+                return 1
+
+        def _gs(user, v):
+            try:
+                v[0] = float(glosum(float(v[0])))
+                return 0
+            except Exception:
+                return 1
+
+        self._ex, self._gs = EXCHANGE_FN(_ex), GLOSUM_FN(_gs)
+
+    def __enter__(self):
+        bs, be, bi = self.args
+        lib().oracle_set_halo(self.Npro, self.NB, _ip(bs), _ip(be), _ip(bi), self._ex, self._gs,
+                              None)
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        failed = lib().oracle_halo_failed()
+        lib().oracle_clear_halo()
+        if failed and exc_type is None:
+            raise RuntimeError("oracle halo: an exchange or global-sum callback failed")
+        return False
 
 
 def solve_system(method, sysm, prec, niter=1000, tol=None, x=None, b=None):

@@ -29,6 +29,16 @@
  * Single-domain run: glosum and Exchng are the identity and the subdomain
  * loops `do sub=1,Npro` have no iterations (Npro = 0 for one rank,
  * Parallel/Double/StaPar.f90:31-34), so the Ab halo terms never contribute.
+ * Subdomain run (oracle_set_halo on the calling thread, one thread or
+ * process per rank): the halo maps of par_mod (NBBs, NBBe, BufInd as
+ * Parallel/Double/BufLoa.f90:35-84 leaves them), Exchng
+ * (Parallel/Double/Exchng.f90:26-62: buffer cells take the values of the
+ * cells they mirror, then the caller's exchange callback swaps each
+ * neighbour's segment, as MPI_SENDRECV_REPLACE does) and glosum (the
+ * caller's sum over ranks, Parallel/Double/GloSum.f90) are called where the
+ * reference calls them, and the halo loops add Ab(k) p(k) to row BufInd(k)
+ * (CG.f90:200-208, BiCG.f90:202-211, CGS.f90:201-208 and :301-308,
+ * Resid.f90:36-42).
  *
  * Array conventions follow the Fortran dummies: 1-based Acol/Arow/Adia;
  * x_base points at x(-NB) and Ab_base at Ab(-NB).
@@ -45,6 +55,78 @@
 /* sol_mod :: error, which outlives a call (Library/sol_mod.f90:9).  One copy
  * per thread: threads stand in for MPI ranks, each with its own module. */
 static _Thread_local double s_error = 0.0;
+
+/* par_mod's halo maps and the rank-coupling callbacks of the calling thread.
+ * exchange(user, phi, NB): phi points at PHI(-NB); swap each neighbour's
+ * segment PHI(NBBe(sub):NBBs(sub)) in place.  glosum(user, v): replace *v by
+ * the sum over ranks.  A nonzero return marks the halo as failed. */
+typedef int (*halo_exchange_fn)(void *user, double *phi, int NB);
+typedef int (*halo_glosum_fn)(void *user, double *value);
+typedef struct {
+    int on, Npro, NB, failed;
+    const int *NBBs, *NBBe; /* NBBs(sub) = NBBs[sub - 1], sub = 1..Npro */
+    const int *BufInd;      /* BufInd(k) = BufInd[k + NB], k = -NB..-1 */
+    halo_exchange_fn exchange;
+    halo_glosum_fn glosum;
+    void *user;
+} HaloCtx;
+static _Thread_local HaloCtx s_halo;
+
+void oracle_set_halo(int Npro, int NB, const int *NBBs, const int *NBBe, const int *BufInd_base,
+                     halo_exchange_fn exchange, halo_glosum_fn glosum, void *user)
+{
+    s_halo.on = 1;
+    s_halo.Npro = Npro;
+    s_halo.NB = NB;
+    s_halo.failed = 0;
+    s_halo.NBBs = NBBs;
+    s_halo.NBBe = NBBe;
+    s_halo.BufInd = BufInd_base;
+    s_halo.exchange = exchange;
+    s_halo.glosum = glosum;
+    s_halo.user = user;
+}
+void oracle_clear_halo(void) { memset(&s_halo, 0, sizeof(s_halo)); }
+int oracle_halo_failed(void) { return s_halo.failed; }
+
+/* Parallel/Double/GloSum.f90 */
+static void glosum(double *v)
+{
+    if (s_halo.on && s_halo.glosum(s_halo.user, v) != 0) s_halo.failed = 1;
+}
+
+/* Parallel/Double/Exchng.f90:26-62 on a vector whose buffer part is
+ * addressable: F1(phi, k) for k = -NB..N. */
+static void exchng(double *phi)
+{
+    if (!s_halo.on) return;
+    for (int sub = 1; sub <= s_halo.Npro; ++sub) {
+        const int s0 = s_halo.NBBs[sub - 1], e0 = s_halo.NBBe[sub - 1];
+        if (e0 <= s0)
+            for (int c2 = s0; c2 >= e0; --c2) F1(phi, c2) = F1(phi, s_halo.BufInd[c2 + s_halo.NB]);
+    }
+    if (s_halo.exchange(s_halo.user, &F1(phi, -s_halo.NB), s_halo.NB) != 0) s_halo.failed = 1;
+}
+
+/* The halo loop after a product: q(BufInd(k)) = q(BufInd(k)) + Ab(k)*p(k),
+ * sub ascending, k from NBBs(sub) down to NBBe(sub). */
+static void halo_add(double *q, const double *p, const double *Ab_base)
+{
+    if (!s_halo.on) return;
+    for (int sub = 1; sub <= s_halo.Npro; ++sub) {
+        const int s0 = s_halo.NBBs[sub - 1], e0 = s_halo.NBBe[sub - 1];
+        if (e0 <= s0)
+            for (int k = s0; k >= e0; --k) {
+                const int i = s_halo.BufInd[k + s_halo.NB];
+                F1(q, i) = F1(q, i) + Ab_base[k + s_halo.NB] * F1(p, k);
+            }
+    }
+}
+
+/* Vectors that are exchanged carry the buffer part in front: F1(v, k) is
+ * valid for k = -NB..N (NB = 0 leaves the one-domain layout unchanged). */
+static double *hvec(int N, int NB) { return (double *)calloc((size_t)N + NB + 2, sizeof(double)) + NB + 1; }
+static void hvec_free(double *v, int NB) { free(v - NB - 1); }
 
 void oracle_reset_state(void) { s_error = 0.0; }
 double oracle_error_state(void) { return s_error; }
@@ -76,11 +158,20 @@ void oracle_resid(int N, int NB, int NONZ, const double *A, const int *Acol,
                   double *r1)
 {
     (void)NONZ;
-    (void)Ab_base;
     for (int i = 1; i <= N; ++i)
         for (int j = F1(Acol, i); j <= F1(Acol, i + 1) - 1; ++j) {
             int k = F1(Arow, j);
             F1(r1, i) = F1(r1, i) - F1(A, j) * x_base[k + NB];
+        }
+    /* Resid.f90:36-42: x's buffer cells as the caller left them (no Exchng) */
+    if (s_halo.on)
+        for (int sub = 1; sub <= s_halo.Npro; ++sub) {
+            const int s0 = s_halo.NBBs[sub - 1], e0 = s_halo.NBBe[sub - 1];
+            if (e0 <= s0)
+                for (int k = s0; k >= e0; --k) {
+                    const int i = s_halo.BufInd[k + NB];
+                    F1(r1, i) = F1(r1, i) - Ab_base[k + NB] * x_base[k + NB];
+                }
         }
 }
 
@@ -127,6 +218,7 @@ static double norm2(int N, const double *r)
 {
     double e = 0.0;
     for (int i = 1; i <= N; ++i) e = e + F1(r, i) * F1(r, i);
+    glosum(&e);
     return sqrt(e);
 }
 
@@ -137,7 +229,7 @@ void oracle_cg(int N, int NB, int NONZ, const double *A, const int *Acol,
                double *IniRes, double *FinRes)
 {
     double *D = calloc((size_t)N + 1, sizeof(double));
-    double *p1 = calloc((size_t)N + 1, sizeof(double));
+    double *p1 = hvec(N, NB);
     double *q1 = calloc((size_t)N + 1, sizeof(double));
     double *x = x_base + NB; /* x[i] == x(i) */
     double rho = 0.0, rhoold = 0.0, alfa, beta, bnrm2;
@@ -173,6 +265,7 @@ void oracle_cg(int N, int NB, int NONZ, const double *A, const int *Acol,
 
         rho = 0.0;
         for (int i = 1; i <= N; ++i) rho = rho + F1(r1, i) * F1(q1, i);
+        glosum(&rho);
 
         if (iter == 1) {
             for (int i = 1; i <= N; ++i) F1(p1, i) = F1(q1, i);
@@ -182,9 +275,12 @@ void oracle_cg(int N, int NB, int NONZ, const double *A, const int *Acol,
         }
 
         spmv(N, A, Acol, Arow, p1, q1);
+        exchng(p1);
+        halo_add(q1, p1, Ab_base);
 
         alfa = 0.0;
         for (int i = 1; i <= N; ++i) alfa = alfa + F1(p1, i) * F1(q1, i);
+        glosum(&alfa);
         alfa = rho / alfa;
 
         for (int i = 1; i <= N; ++i) {
@@ -202,7 +298,7 @@ done:
     *FinRes = s_error;
     *niter = iter;
     free(D);
-    free(p1);
+    hvec_free(p1, NB);
     free(q1);
 }
 
@@ -215,7 +311,7 @@ void oracle_bicg(int N, int NB, int NONZ, const double *A, const int *Acol,
 {
     size_t n1 = (size_t)N + 1;
     double *D = calloc(n1, sizeof(double));
-    double *p1 = calloc(n1, sizeof(double)), *p2 = calloc(n1, sizeof(double));
+    double *p1 = hvec(N, NB), *p2 = hvec(N, NB);
     double *q1 = calloc(n1, sizeof(double)), *q2 = calloc(n1, sizeof(double));
     double *r2 = calloc(n1, sizeof(double));
     double *x = x_base + NB;
@@ -262,6 +358,7 @@ void oracle_bicg(int N, int NB, int NONZ, const double *A, const int *Acol,
 
         rho = 0.0;
         for (int i = 1; i <= N; ++i) rho = rho + F1(q1, i) * F1(r2, i);
+        glosum(&rho);
 
         if (iter == 1) {
             for (int i = 1; i <= N; ++i) {
@@ -278,9 +375,14 @@ void oracle_bicg(int N, int NB, int NONZ, const double *A, const int *Acol,
 
         spmv(N, A, Acol, Arow, p1, q1);
         spmv(N, A, Acol, Arow, p2, q2);
+        exchng(p1);
+        exchng(p2);
+        halo_add(q1, p1, Ab_base);
+        halo_add(q2, p2, Ab_base);
 
         alfa = 0.0;
         for (int i = 1; i <= N; ++i) alfa = alfa + F1(p2, i) * F1(q1, i);
+        glosum(&alfa);
         alfa = rho / alfa;
 
         for (int i = 1; i <= N; ++i) {
@@ -299,8 +401,8 @@ done:
     *FinRes = s_error;
     *niter = iter;
     free(D);
-    free(p1);
-    free(p2);
+    hvec_free(p1, NB);
+    hvec_free(p2, NB);
     free(q1);
     free(q2);
     free(r2);
@@ -314,7 +416,7 @@ void oracle_cgs(int N, int NB, int NONZ, const double *A, const int *Acol,
 {
     size_t n1 = (size_t)N + 1;
     double *D = calloc(n1, sizeof(double));
-    double *p1 = calloc(n1, sizeof(double)), *p2 = calloc(n1, sizeof(double));
+    double *p1 = hvec(N, NB), *p2 = hvec(N, NB);
     double *q1 = calloc(n1, sizeof(double)), *q2 = calloc(n1, sizeof(double));
     double *r2 = calloc(n1, sizeof(double));
     double *u1 = calloc(n1, sizeof(double)), *u2 = calloc(n1, sizeof(double));
@@ -345,6 +447,7 @@ void oracle_cgs(int N, int NB, int NONZ, const double *A, const int *Acol,
     for (iter = 1; iter <= *niter; ++iter) {
         rho = 0.0;
         for (int i = 1; i <= N; ++i) rho = rho + F1(r1, i) * F1(r2, i);
+        glosum(&rho);
 
         if (iter == 1) {
             for (int i = 1; i <= N; ++i) {
@@ -371,9 +474,12 @@ void oracle_cgs(int N, int NB, int NONZ, const double *A, const int *Acol,
         /* v2 = A p2 (CGS.f90:193-200; the stray alfa sum at :199 is
          * overwritten at :215 and changes nothing) */
         spmv(N, A, Acol, Arow, p2, v2);
+        exchng(p2);
+        halo_add(v2, p2, Ab_base);
 
         alfa = 0.0;
         for (int i = 1; i <= N; ++i) alfa = alfa + F1(r2, i) * F1(v2, i);
+        glosum(&alfa);
         alfa = rho / alfa;
 
         for (int i = 1; i <= N; ++i) F1(q1, i) = F1(u1, i) - alfa * F1(v2, i);
@@ -392,6 +498,8 @@ void oracle_cgs(int N, int NB, int NONZ, const double *A, const int *Acol,
         for (int i = 1; i <= N; ++i) x[i] = x[i] + alfa * F1(p1, i);
 
         spmv(N, A, Acol, Arow, p1, q2);
+        exchng(p1);
+        halo_add(q2, p1, Ab_base);
 
         for (int i = 1; i <= N; ++i) F1(r1, i) = F1(r1, i) - alfa * F1(q2, i);
 
@@ -405,8 +513,8 @@ done:
     *FinRes = s_error;
     *niter = iter;
     free(D);
-    free(p1);
-    free(p2);
+    hvec_free(p1, NB);
+    hvec_free(p2, NB);
     free(q1);
     free(q2);
     free(r2);

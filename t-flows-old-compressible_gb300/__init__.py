@@ -10,8 +10,9 @@ from . import mesh  # noqa: F401
 from ._native import LIB_PATH, NativeLibraryError, build as build_library, header_symbols  # noqa: F401
 from ._native import load as load_library  # noqa: F401
 from .api import (  # noqa: F401
-    BAD_INPUT, BICG, BICG_TRUE, BREAKDOWN, CG, CGS, CUDA_ERROR, FP64, FP64_FMA, MIXED, NO_DEVICE, NONFINITE,
+    BAD_INPUT, BICG, BICG_TRUE, BREAKDOWN, CG, CGS, CUDA_ERROR, FP64, FP64_FMA, HALO_ERROR, MIXED,
+    NO_DEVICE, NONFINITE,
     NOT_CONVERGED, OK, TIMEOUT, TOL_ABSOLUTE, TOL_RELATIVE, UNSUPPORTED, SolveOutput, SolverError,
-    Assembly, Plan, Topology, autotune_clear, bicg, cg, cgs, finalize, last_error, last_result, last_status, options, prec1, resid,
-    read_mesh, set_options, solve_batched, solve_ex, solve_system, status_string, topolm,
+    Assembly, Plan, Topology, autotune_clear, bicg, cg, cgs, clear_halo, finalize, last_error, last_result, last_status, options, prec1, resid,
+    read_mesh, set_halo, set_options, solve_batched, solve_ex, solve_system, status_string, topolm,
 )

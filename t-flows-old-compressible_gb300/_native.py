@@ -19,7 +19,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libtflows_krylov.so")
 SOURCES = ("krylov.cu", "krylov_fma.cu", "shim.cu", "noalloc.cu", "tune.cu", "assembly.cu",
-           "momentum.cu", "meshio.cpp")
+           "momentum.cu", "halo.cu", "meshio.cpp")
 HEADERS = ("device_common.cuh", "krylov_kernels.cuh", "solver_entry.cuh", "internal.h",
            "assembly_internal.h")
 
@@ -165,6 +165,9 @@ class NewuvwParams(ctypes.Structure):
 
 
 _SOLVER = [_I, _I, _I, _D, _I, _I, _I, _D, _D, _D, _I, _I, _D, _D, _D]
+# tflows_exchange_fn / tflows_glosum_fn
+EXCHANGE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, _D, ctypes.c_int)
+GLOSUM_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, _D)
 
 SIGNATURES = {
     "tflows_default_options": ([ctypes.POINTER(Options)], None),
@@ -179,6 +182,9 @@ SIGNATURES = {
     "tflows_last_error": ([], ctypes.c_char_p),
     "tflows_last_result": ([ctypes.POINTER(Result)], None),
     "tflows_finalize": ([], None),
+    "tflows_set_halo": ([ctypes.c_int, ctypes.c_int, _I, _I, _I, EXCHANGE_FN, GLOSUM_FN, _VP],
+                        ctypes.c_int),
+    "tflows_clear_halo": ([], None),
     "tflows_solve_ex": ([ctypes.c_int, *_SOLVER, ctypes.POINTER(Options), ctypes.POINTER(Result)],
                         ctypes.c_int),
     "tflows_topology_create": ([ctypes.POINTER(_VP), ctypes.c_int, ctypes.c_int, _VP, _VP, _VP,

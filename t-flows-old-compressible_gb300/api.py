@@ -22,8 +22,8 @@ import numpy as np
 
 from . import _native
 
-OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT, BAD_INPUT, CUDA_ERROR, NO_DEVICE, UNSUPPORTED = \
-    range(9)
+(OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT, BAD_INPUT, CUDA_ERROR, NO_DEVICE, UNSUPPORTED,
+ HALO_ERROR) = range(10)
 CG, BICG, CGS, BICG_TRUE = 0, 1, 2, 3
 FP64, MIXED, FP64_FMA = 0, 1, 2
 TOL_ABSOLUTE, TOL_RELATIVE = 0, 1
@@ -141,6 +141,56 @@ def _legacy(method):
     fn.__doc__ = (f"The reference's `{method}` (Process/{ {'cg': 'CG', 'bicg': 'BiCG', 'cgs': 'CGS'}[method]}.f90) "
                   "on the GPU: x and r1 updated in place; returns (niter, IniRes, FinRes, status).")
     return fn
+
+
+_halo_keep = None
+
+
+def set_halo(Npro, NB, NBBs, NBBe, BufInd, exchange, glosum):
+    """tflows_set_halo: register this rank's subdomain halo for the
+    Fortran-facing entry points (the reference's Npro > 0 run).
+
+    ``NBBs``, ``NBBe``: Npro entries, NBBs(sub) and NBBe(sub) for sub = 1..Npro
+    as Parallel/Double/BufLoa.f90 leaves them; ``BufInd``: BufInd(-NB:-1)
+    (length NB).  ``exchange(phi)`` receives the float64 array PHI(-NB:-1)
+    (``phi[NB + k]`` = PHI(k)) whose buffer cells hold the values of the
+    cells they mirror and must swap each neighbour's segment
+    PHI(NBBe(sub):NBBs(sub)) with rank sub-1 in place; ``glosum(v)`` returns
+    the sum of ``v`` over the ranks.  An exception in either ends the solve
+    with HALO_ERROR."""
+    global _halo_keep
+    bs = np.ascontiguousarray(NBBs, dtype=np.int32)
+    be = np.ascontiguousarray(NBBe, dtype=np.int32)
+    bi = np.ascontiguousarray(BufInd if NB > 0 else np.zeros(1), dtype=np.int32)
+
+    def _ex(user, phi, nb):
+        try:
+            exchange(np.ctypeslib.as_array(phi, shape=(nb,)))
+            return 0
+        except Exception:  # reported to the solver as a failed exchange
+            return 1
+
+    def _gs(user, v):
+        try:
+            v[0] = float(glosum(float(v[0])))
+            return 0
+        except Exception:  # reported to the solver as a failed sum
+            return 1
+
+    ex, gs = _native.EXCHANGE_FN(_ex), _native.GLOSUM_FN(_gs)
+    ip = ctypes.POINTER(ctypes.c_int)
+    st = lib().tflows_set_halo(int(Npro), int(NB), bs.ctypes.data_as(ip), be.ctypes.data_as(ip),
+                               bi.ctypes.data_as(ip), ex, gs, None)
+    if st != OK:
+        raise SolverError(st, last_error())
+    _halo_keep = (ex, gs)  # the library calls them until the halo is cleared
+
+
+def clear_halo():
+    """tflows_clear_halo: back to the one-domain run (Ab not read)."""
+    global _halo_keep
+    lib().tflows_clear_halo()
+    _halo_keep = None
 
 
 cg = _legacy("cg")

@@ -176,6 +176,16 @@ cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, con
 // Records the status and message tflows_last_status / tflows_last_error report.
 int report_status(int status, const std::string& msg);
 
+// Subdomain-coupled solves (halo.cu): whether a halo is registered, the
+// coupled solve of the Fortran-facing entry points and the coupled Resid.
+bool halo_registered();
+int halo_solve(int method, int n, int nb, int nonz, const double* A, const int* Acol,
+               const int* Arow, const int* Adia, const double* Ab, double* x, double* r1,
+               int prec, int* niter, double tol, double* IniRes, double* FinRes,
+               double& error_state, cudaStream_t s, SolveReport& rep);
+int halo_resid(int n, int nb, int nonz, const double* A, const int* Acol, const int* Arow,
+               const double* Ab, const double* x, double* r1, cudaStream_t s, std::string& msg);
+
 // The persistent kernels, built twice: krylov.cu with the reference's
 // arithmetic (separate rounded products and sums, dividing diagonal) and
 // krylov_fma.cu with fused multiply-adds (TFLOWS_FP64_FMA and mixed solves).

@@ -644,6 +644,7 @@ const char* tflows_status_string(int s) {
         case TFLOWS_CUDA_ERROR: return "CUDA error";
         case TFLOWS_NO_DEVICE: return "no CUDA device";
         case TFLOWS_UNSUPPORTED: return "unsupported option";
+        case TFLOWS_HALO_ERROR: return "halo callback failed";
         default: return "unknown status";
     }
 }
@@ -668,7 +669,6 @@ int tflows_solve_ex(int method, const int* N, const int* NB, const int* NONZ, co
                     const int* Acol, const int* Arow, const int* Adia, const double* Ab, double* x,
                     double* r1, const int* prec, int* niter, const double* tol, double* IniRes,
                     double* FinRes, const tflows_options* opt, tflows_result* res) {
-    (void)Ab;  // halo coefficients: no subdomain neighbours in a one-domain run
     t_error.clear();
     SolveReport rep;
     if (!N || !NB || !NONZ || !prec || !niter || !tol || !IniRes || !FinRes || !x || !r1) {
@@ -705,6 +705,18 @@ int tflows_solve_ex(int method, const int* N, const int* NB, const int* NONZ, co
     if (!A || !Acol || !Arow || !Adia) return fail(TFLOWS_BAD_INPUT, "null matrix array");
     int st = set_device(c, o.device);
     if (st != TFLOWS_OK) return st;
+    if (halo_registered()) {
+        // subdomain run: Ab couples the rows to the neighbours' buffer cells
+        if (o.precision != TFLOWS_FP64)
+            return fail(TFLOWS_UNSUPPORTED, "halo-coupled solves run in FP64 reference arithmetic");
+        st = halo_solve(method, n, nb, nonz, A, Acol, Arow, Adia, Ab, x, r1, *prec, niter, *tol,
+                        IniRes, FinRes, c.error_state, c.stream, rep);
+        record(rep, res);
+        t_status = st;
+        t_error = rep.message;
+        return st;
+    }
+    // one-domain run (Npro = 0): the subdomain loops are empty and Ab is not read
     tflows_topology* tp = nullptr;
     st = cached_topology(c, n, nonz, Acol, Arow, Adia, &tp);
     if (st != TFLOWS_OK) return st;
@@ -806,7 +818,6 @@ void tflows_prec1(const int* N, const int* NONZ, const double* A, const int* Aco
 
 void tflows_resid(const int* N, const int* NB, const int* NONZ, const double* A, const int* Acol,
                   const int* Arow, const double* Ab, const double* x, double* r1) {
-    (void)Ab;
     t_error.clear();
     if (!N || !NB || !NONZ || !x || !r1) { fail(TFLOWS_BAD_INPUT, "null argument"); return; }
     const int n = *N, nb = *NB;
@@ -815,6 +826,15 @@ void tflows_resid(const int* N, const int* NB, const int* NONZ, const double* A,
     std::lock_guard<std::mutex> lk(c.mu);
     int st = set_device(c, c.opts_set ? c.opts.device : -1);
     if (st != TFLOWS_OK) return;
+    if (halo_registered()) {
+        // subdomain run: r1(BufInd(k)) -= Ab(k) x(k) after the local rows
+        std::string msg;
+        if (!A || !Acol || !Arow) { fail(TFLOWS_BAD_INPUT, "null matrix array"); return; }
+        st = halo_resid(n, nb, *NONZ, A, Acol, Arow, Ab, x, r1, c.stream, msg);
+        if (st != TFLOWS_OK) { fail(st, msg); return; }
+        t_status = TFLOWS_OK;
+        return;
+    }
     // Resid needs no diagonal positions; a pattern without Adia gets a
     // synthesised one so that the cache and layout can be shared.
     tflows_topology* tp = nullptr;

@@ -602,3 +602,108 @@ def structured_levels(nx, ny, nz):
     N = nx * ny * nz
     cell = np.arange(N, dtype=np.int64)
     return (cell % nx) + (cell // nx) % ny + cell // (nx * ny)
+
+
+@dataclasses.dataclass
+class Subdomain:
+    """One rank's part of a system split into subdomains, in the layout a
+    T-FlowS rank holds after Parallel/Double/BufLoa.f90:35-84.
+
+    Rows are the rank's cells (``rows`` their global 0-based indices, in
+    order); the matrix keeps the local couplings, and each coupling to a
+    cell of neighbour ``sub`` becomes a buffer cell k (negative, inside
+    x(-NB:-1)) with ``Ab`` holding the coefficient and ``BufInd`` the local
+    row: ``Ab[NB + k]`` = Ab(k), ``BufInd[NB + k]`` = BufInd(k).  ``NBBs``,
+    ``NBBe`` hold NBBs(sub), NBBe(sub) for sub = 1..Npro; the first
+    ``n_phys`` boundary cells x(-n_phys:-1) stand for the physical boundary
+    cells and carry no coupling.  Both sides of a neighbour pair order their
+    shared couplings by the global (row, column) of the lower-numbered side,
+    so that the k-th cell of one rank's segment meets the k-th of the
+    other's when the segments are swapped."""
+
+    rank: int
+    Npro: int
+    N: int
+    NB: int
+    NONZ: int
+    A: np.ndarray
+    Acol: np.ndarray
+    Arow: np.ndarray
+    Adia: np.ndarray
+    Ab: np.ndarray
+    b: np.ndarray
+    x: np.ndarray
+    NBBs: np.ndarray
+    NBBe: np.ndarray
+    BufInd: np.ndarray
+    rows: np.ndarray
+
+    def segments(self):
+        """(partner rank, lo, hi) slices of the PHI(-NB:-1) array that are
+        exchanged with each connected neighbour, in neighbour order."""
+        out = []
+        for sub in range(1, self.Npro + 1):
+            s0, e0 = int(self.NBBs[sub - 1]), int(self.NBBe[sub - 1])
+            if e0 <= s0:
+                out.append((sub - 1, self.NB + e0, self.NB + s0 + 1))
+        return out
+
+
+def partition(s: System, nparts: int, n_phys: int = 2) -> list:
+    """Split ``s`` into ``nparts`` subdomains of consecutive rows (slabs of
+    a box in natural numbering), returning one Subdomain per rank."""
+    N = s.N
+    rp = s.Acol.astype(np.int64) - 1
+    col = s.Arow[:-1].astype(np.int64) - 1
+    val = s.A[:-1]
+    owner = (np.arange(N) * nparts) // N
+    subs = []
+    for r in range(nparts):
+        rows = np.nonzero(owner == r)[0]
+        loc = np.full(N, -1, np.int64)
+        loc[rows] = np.arange(rows.size)
+        Acol = [1]
+        Arow, A, Adia = [], [], []
+        links = {q: [] for q in range(nparts) if q != r}  # (key, local row, coefficient)
+        for i in rows:
+            for j in range(rp[i], rp[i + 1]):
+                c = col[j]
+                if owner[c] == r:
+                    if c == i:
+                        Adia.append(len(A) + 1)
+                    Arow.append(loc[c] + 1)
+                    A.append(val[j])
+                else:
+                    links[owner[c]].append(((min(i, c), max(i, c)), loc[i] + 1, val[j]))
+            Acol.append(len(A) + 1)
+        nbuf = sum(len(v) for v in links.values())
+        NB = n_phys + nbuf
+        NBBs = np.zeros(nparts, np.int32)
+        NBBe = np.zeros(nparts, np.int32)
+        Ab = np.zeros(NB)
+        BufInd = np.zeros(NB, np.int32)
+        prev_e = -n_phys  # NBBe(0) = -NBC (BufLoa.f90:47-50)
+        for sub in range(1, nparts + 1):
+            q = sub - 1
+            lst = sorted(links.get(q, []), key=lambda t: t[0])
+            if q == r or not lst:
+                NBBs[q], NBBe[q] = prev_e - 1, prev_e  # empty: NBBe > NBBs
+                continue
+            s0 = prev_e - 1
+            e0 = s0 - len(lst) + 1
+            for m, (_, i_loc, a) in enumerate(lst):
+                k = s0 - m
+                Ab[NB + k] = a
+                BufInd[NB + k] = i_loc
+            NBBs[q], NBBe[q] = s0, e0
+            prev_e = e0
+        for q in range(nparts):  # BufLoa.f90:74-80: empty ranges become (-1, 0)
+            if NBBe[q] > NBBs[q]:
+                NBBs[q], NBBe[q] = -1, 0
+        A = np.array(A + [0.0])
+        subs.append(Subdomain(
+            rank=r, Npro=nparts, N=int(rows.size), NB=NB, NONZ=len(A), A=A,
+            Acol=np.array(Acol, np.int32), Arow=np.array(Arow + [0], np.int32),
+            Adia=np.array(Adia, np.int32), Ab=Ab, b=s.b[rows].copy(),
+            x=np.zeros(NB + 1 + rows.size), NBBs=NBBs, NBBe=NBBe, BufInd=BufInd, rows=rows))
+    return subs
