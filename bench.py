@@ -471,9 +471,49 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
                                if kk not in ("group_blocks", "iterations", "rel_err_vs_tight_fp64")}
                            for k, v in variants.items()}
     out["tight_fp64_converged"] = tight_ok
+    out["cpu_baseline"] = cfg4_cpu_estimate(pkg, dev, systems, topos, vals, bs)
     for tp in topos:
         tp.close()
     return out
+
+
+def cfg4_cpu_estimate(pkg, dev, systems, topos, vals, bs, iters=2):
+    """The oracle on the batch, one solve per host core.  Each system's
+    oracle solve is its set-up (an oracle run with no iterations) plus
+    `iters` whole iterations, scaled to the iteration count of the
+    reference-arithmetic GPU solve of the same system at the same tolerance
+    (the same algorithm; its counts match the oracle's within 1); the
+    estimates are then placed longest first on the least-loaded core."""
+    import numpy as np
+    import torch
+    import oracle
+    ref = pkg.options(precision=pkg.FP64, tol_mode=pkg.TOL_RELATIVE)
+    est, its = [], []
+    for (sy, m, p), tp, v, bb in zip(systems, topos, vals, bs):
+        xt = torch.zeros(sy.N, dtype=torch.float64, device=dev)
+        r = tp.solve(v, bb, xt, m, p, 20000, 1e-8, opts=ref, raise_on_error=False)
+        tol = 1e-8 * float(np.linalg.norm(sy.b))
+        t0 = time.perf_counter()
+        oracle.solve(m, sy.N, sy.NB, sy.NONZ, sy.A, sy.Acol, sy.Arow, sy.Adia, sy.Ab, sy.x, sy.b,
+                     p, 0, tol)
+        t1 = time.perf_counter()
+        oracle.solve(m, sy.N, sy.NB, sy.NONZ, sy.A, sy.Acol, sy.Arow, sy.Adia, sy.Ab, sy.x, sy.b,
+                     p, iters, tol)
+        t2 = time.perf_counter()
+        t_it = max((t2 - t1) - (t1 - t0), 0.0) / iters
+        its.append(r["iterations"])
+        est.append((t1 - t0) + r["iterations"] * t_it)
+    cores = os.cpu_count() or 1
+    loads = [0.0] * cores
+    for t in sorted(est, reverse=True):
+        k = loads.index(min(loads))
+        loads[k] += t
+    return {"seconds_per_batch": max(loads), "systems_per_s": len(est) / max(loads),
+            "one_core_seconds": sum(est), "cores": cores, "kind": "port",
+            "sample": f"per system the oracle's set-up and {iters} whole iterations, scaled to the "
+                      "iteration count of the reference-arithmetic GPU solve at 1e-8 relative; "
+                      f"the {len(est)} solves placed longest first on {cores} host cores",
+            "iterations_fp64": its}
 
 
 def legacy_e2e(pkg, s, method, prec, opts_kw, steps, warmup):
@@ -701,11 +741,25 @@ def adjoint_cfg5(pkg, dev, reps=3):
     ms = e0.elapsed_time(e1) / reps
     fw, bw = solver.last_forward, solver.last_adjoint
     solver.topo.close()
+    # CPU baseline: the oracle's forward solve and its adjoint solve (the
+    # system is symmetric, so the transposed solve is a CG on A with the
+    # loss gradient as right-hand side), one host core each, timed whole
+    import oracle
+    t0 = time.perf_counter()
+    xo, _, it_f, _, _ = oracle.solve("cg", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
+                                     s.x, s.b, 1, 20000, 1e-10 * float(np.linalg.norm(s.b)))
+    t1 = time.perf_counter()
+    g = xo[s.NB + 1:] - xt.cpu().numpy()
+    _, _, it_a, _, _ = oracle.solve("cg", s.N, s.NB, s.NONZ, s.A, s.Acol, s.Arow, s.Adia, s.Ab,
+                                    s.x, g, 1, 20000, 1e-10 * float(np.linalg.norm(g)))
+    t2 = time.perf_counter()
     return {"workload": f"{s.name} differentiable CG + diagonal, rtol 1e-10, loss 0.5||x-x_t||^2",
             "n": s.N, "ms_per_forward_backward": ms,
             "forward": {"iterations": fw["iterations"], "ms": 1e3 * fw["seconds"]},
             "adjoint": {"iterations": bw["iterations"], "ms": 1e3 * bw["seconds"]},
-            "grad_b_norm": float(b.grad.norm()), "grad_coef_norm": float(coef.grad.norm())}
+            "grad_b_norm": float(b.grad.norm()), "grad_coef_norm": float(coef.grad.norm()),
+            "cpu_oracle_1core": {"forward_ms": 1e3 * (t1 - t0), "forward_iterations": it_f,
+                                 "adjoint_ms": 1e3 * (t2 - t1), "adjoint_iterations": it_a}}
 
 
 def simple_step(pkg, dev, n=128, reps=3, autotune=True):
