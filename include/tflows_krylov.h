@@ -178,6 +178,11 @@ const char *tflows_status_string(int status);
 const char *tflows_last_error(void);
 /* Result details of the last solve made on this thread. */
 void tflows_last_result(tflows_result *res);
+/* Drop the device copies of Acol/Arow/Adia that the legacy calls keep,
+ * keyed by the arrays' addresses, sizes and a sampled content hash; call it
+ * after rewriting those arrays in place (or set TFLOWS_TOPOLOGY_CHECK=full
+ * to hash every element). */
+void tflows_forget_topologies(void);
 /* Release every device resource the library holds. */
 void tflows_finalize(void);
 

@@ -13,6 +13,6 @@ from .api import (  # noqa: F401
     BAD_INPUT, BICG, BICG_TRUE, BREAKDOWN, CG, CGS, CUDA_ERROR, FP64, FP64_FMA, HALO_ERROR, MIXED,
     NO_DEVICE, NONFINITE,
     NOT_CONVERGED, OK, TIMEOUT, TOL_ABSOLUTE, TOL_RELATIVE, UNSUPPORTED, SolveOutput, SolverError,
-    Assembly, Plan, Topology, autotune_clear, bicg, cg, cgs, clear_halo, finalize, last_error, last_result, last_status, options, prec1, resid,
+    Assembly, Plan, Topology, autotune_clear, bicg, cg, cgs, clear_halo, finalize, forget_topologies, last_error, last_result, last_status, options, prec1, resid,
     read_mesh, set_halo, set_options, solve_batched, solve_ex, solve_system, status_string, topolm,
 )

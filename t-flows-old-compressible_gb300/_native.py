@@ -182,6 +182,7 @@ SIGNATURES = {
     "tflows_last_error": ([], ctypes.c_char_p),
     "tflows_last_result": ([ctypes.POINTER(Result)], None),
     "tflows_finalize": ([], None),
+    "tflows_forget_topologies": ([], None),
     "tflows_set_halo": ([ctypes.c_int, ctypes.c_int, _I, _I, _I, EXCHANGE_FN, GLOSUM_FN, _VP],
                         ctypes.c_int),
     "tflows_clear_halo": ([], None),

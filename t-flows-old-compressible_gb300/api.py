@@ -83,6 +83,12 @@ def finalize() -> None:
     lib().tflows_finalize()
 
 
+def forget_topologies() -> None:
+    """tflows_forget_topologies: drop the legacy calls' cached device
+    patterns (after the caller rewrote Acol/Arow/Adia in place)."""
+    lib().tflows_forget_topologies()
+
+
 def autotune_clear() -> None:
     """Forget every tuned launch shape of this process."""
     lib().tflows_autotune_clear()

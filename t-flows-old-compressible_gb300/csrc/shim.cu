@@ -655,6 +655,14 @@ void tflows_last_result(tflows_result* res) {
     if (res) *res = t_result;
 }
 
+void tflows_forget_topologies(void) {
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (c.device >= 0) cudaSetDevice(c.device);
+    for (auto& tp : c.cache) destroy_topo(tp.get());
+    c.cache.clear();
+}
+
 void tflows_finalize(void) {
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
