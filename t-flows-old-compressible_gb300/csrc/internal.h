@@ -175,6 +175,8 @@ cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, con
 
 // Records the status and message tflows_last_status / tflows_last_error report.
 int report_status(int status, const std::string& msg);
+// Host-time phase mark of a legacy call run with TFLOWS_TRACE_LEGACY set.
+void trace_mark(const char* what);
 
 // Subdomain-coupled solves (halo.cu): whether a halo is registered, the
 // coupled solve of the Fortran-facing entry points and the coupled Resid.

@@ -685,14 +685,17 @@ int launch_and_report(K kern, P& params, const DeviceTopology& t, Workspace& ws,
     const int block = block_of(rq);
     const unsigned smem = tile_smem_for(t, rq);
     const int grid = choose_grid(t, rq, max_coresident(kern, block, smem));
+    trace_mark("set-up enqueued");
     cudaEventRecord(ws.ev0, s);
     if (e == cudaSuccess) e = launch_coop(kern, params, grid, block, s, smem);
     rep.block = block;
     rep.grid = grid;
     cudaEventRecord(ws.ev1, s);
+    trace_mark("solver launched");
     DevState st;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ws.state, sizeof(st), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    trace_mark("solver finished");
     if (e != cudaSuccess) {
         rep.status = ST_CUDA_ERROR;
         rep.message = std::string("solver: ") + cudaGetErrorString(e);

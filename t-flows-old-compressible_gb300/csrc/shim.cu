@@ -9,6 +9,7 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <chrono>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -579,10 +580,12 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
     if (rq.method == TFLOWS_METHOD_BICG_TRUE &&
         (e = permute_transposed(tp->t, tp->ws, d_val, s)) != cudaSuccess)
         return cuda_fail(e, "transposed values");
+    trace_mark("layout enqueued");
     if (rq.autotune) {
         TuneChoice ch;
         if (int st = autotune_on(tp, rq, d_b, d_x, s, ch); st != TFLOWS_OK) return st;
     }
+    trace_mark("launch shape");
     // The kernels work on padded, 16-byte aligned workspace vectors: x and b
     // are staged into workspace slots 11 and 12 unless they already are them.
     const size_t nb = sizeof(double) * tp->t.n;
@@ -611,6 +614,34 @@ int tflows::report_status(int status, const std::string& msg) {
     t_status = status;
     t_error = msg;
     return status;
+}
+
+namespace {
+// TFLOWS_TRACE_LEGACY=1: the legacy calls print the host time at each phase
+// (topology lookup, uploads enqueued, solve returned, results copied back).
+struct LegacyTrace {
+    const bool on = [] {
+        const char* v = std::getenv("TFLOWS_TRACE_LEGACY");
+        return v && *v && *v != '0';
+    }();
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    LegacyTrace();
+    ~LegacyTrace();
+    void mark(const char* what) const {
+        if (!on) return;
+        const double ms = std::chrono::duration<double, std::milli>(
+                              std::chrono::steady_clock::now() - t0).count();
+        std::fprintf(stderr, "tflows legacy: %-22s %10.3f ms\n", what, ms);
+    }
+};
+thread_local const LegacyTrace* t_trace = nullptr;
+LegacyTrace::LegacyTrace() { if (on) t_trace = this; }
+LegacyTrace::~LegacyTrace() { if (t_trace == this) t_trace = nullptr; }
+}  // namespace
+
+// Phase marks from inside a traced legacy call (no-op otherwise).
+void tflows::trace_mark(const char* what) {
+    if (t_trace) t_trace->mark(what);
 }
 
 extern "C" {
@@ -673,6 +704,7 @@ void tflows_finalize(void) {
     c.device = -1;
 }
 
+
 int tflows_solve_ex(int method, const int* N, const int* NB, const int* NONZ, const double* A,
                     const int* Acol, const int* Arow, const int* Adia, const double* Ab, double* x,
                     double* r1, const int* prec, int* niter, const double* tol, double* IniRes,
@@ -711,6 +743,7 @@ int tflows_solve_ex(int method, const int* N, const int* NB, const int* NONZ, co
         return TFLOWS_OK;
     }
     if (!A || !Acol || !Arow || !Adia) return fail(TFLOWS_BAD_INPUT, "null matrix array");
+    const LegacyTrace trace;
     int st = set_device(c, o.device);
     if (st != TFLOWS_OK) return st;
     if (halo_registered()) {
@@ -728,6 +761,7 @@ int tflows_solve_ex(int method, const int* N, const int* NB, const int* NONZ, co
     tflows_topology* tp = nullptr;
     st = cached_topology(c, n, nonz, Acol, Arow, Adia, &tp);
     if (st != TFLOWS_OK) return st;
+    trace.mark("topology");
     cudaError_t e = ensure_workspace(tp->ws, tp->t);
     if (e != cudaSuccess) return cuda_fail(e, "workspace");
     cudaStream_t s = c.stream;
@@ -741,8 +775,11 @@ int tflows_solve_ex(int method, const int* N, const int* NB, const int* NONZ, co
         return cuda_fail(e, "copy x");
     if ((e = cudaMemcpyAsync(B, r1, nbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
         return cuda_fail(e, "copy r1");
+    if (trace.on) cudaStreamSynchronize(s);
+    trace.mark("uploads done");
     SolveRequest rq = make_request(o, method, *prec, *niter, *tol);
     st = solve_on(tp, rq, tp->ws.csr_val, B, X, nullptr, s, rep);
+    trace.mark("solve returned");
     if (st == TFLOWS_CUDA_ERROR || st == TFLOWS_BAD_INPUT || st == TFLOWS_UNSUPPORTED) {
         record(rep, res);
         return st;
@@ -755,6 +792,7 @@ int tflows_solve_ex(int method, const int* N, const int* NB, const int* NONZ, co
         if ((e = cudaMemcpyAsync(r1, R, nbytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
             return cuda_fail(e, "copy r1 back");
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "sync");
+        trace.mark("results copied back");
     }
     *niter = rep.iterations;
     if (untouched) {
