@@ -94,3 +94,56 @@ def test_coupled_ic_solve_converges_to_one_domain_solution(method):
         x[rows] = xl
         assert fin < tol and it < 5000
     assert np.abs(x - xo).max() <= 1e-6 * np.abs(xo).max()
+
+
+def test_set_halo_validates_maps_on_the_host():
+    """tflows_set_halo checks its maps before any device work: ranges
+    outside -NB..-1 and missing callbacks are rejected, an empty neighbour
+    (NBBe > NBBs) is accepted, and Npro = 0 clears the registration."""
+    import ctypes
+    L = tflows.load_library()
+    ip = ctypes.POINTER(ctypes.c_int)
+    ex = tflows._native.EXCHANGE_FN(lambda user, phi, nb: 0)
+    gs = tflows._native.GLOSUM_FN(lambda user, v: 0)
+
+    def call(nbbs, nbbe, NB, exch=ex, gsum=gs):
+        bs = np.array(nbbs, np.int32)
+        be = np.array(nbbe, np.int32)
+        bi = np.ones(max(NB, 1), np.int32)
+        return L.tflows_set_halo(len(nbbs), NB, bs.ctypes.data_as(ip), be.ctypes.data_as(ip),
+                                 bi.ctypes.data_as(ip), exch, gsum, None)
+
+    try:
+        assert call([-3, -1], [-6, 0], 6) == tflows.OK           # neighbour 2 empty
+        assert call([-3, -1], [-7, 0], 6) == tflows.BAD_INPUT    # below -NB
+        assert call([0, -1], [-2, 0], 6) == tflows.BAD_INPUT     # NBBs(1) not negative
+        assert call([-3], [-6], 6, exch=tflows._native.EXCHANGE_FN()) == tflows.BAD_INPUT
+        assert "halo" in tflows.last_error()
+    finally:
+        tflows.clear_halo()
+    bs = np.zeros(1, np.int32)
+    assert L.tflows_set_halo(0, 0, bs.ctypes.data_as(ip), bs.ctypes.data_as(ip), None,
+                             ex, gs, None) == tflows.OK
+
+
+def test_partition_layout_follows_bufloa():
+    """mesh.partition: buffer ranges descend from -(n_phys+1) in neighbour
+    order, connected pairs have equal segment lengths, every buffer cell
+    maps to a local row, and the local matrices keep every entry once."""
+    s = _system()
+    subs = mesh.partition(s, 3)
+    assert sum(d.N for d in subs) == s.N
+    assert sum(d.NONZ - 1 for d in subs) + sum(
+        int((d.BufInd > 0).sum()) for d in subs) == s.NONZ - 1
+    for d in subs:
+        first = True
+        for q, lo, hi in d.segments():
+            assert hi > lo
+            if first:
+                assert hi == d.NB - 2  # below the two physical boundary cells
+                first = False
+            other = subs[q]
+            seg = [sg for sg in other.segments() if sg[0] == d.rank]
+            assert seg and seg[0][2] - seg[0][1] == hi - lo
+            assert np.all((d.BufInd[lo:hi] >= 1) & (d.BufInd[lo:hi] <= d.N))
+        assert d.NBBs[d.rank] == -1 and d.NBBe[d.rank] == 0  # no connection with itself
