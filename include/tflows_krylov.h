@@ -9,7 +9,9 @@
  * x(-NB) and Ab at Ab(-NB).  They mirror the reference outputs: x, r1 (the
  * final recursive residual), niter (iterations used, or niter_in+1 when the
  * tolerance was not reached), IniRes, FinRes.  Nothing here aborts the
- * calling process; tflows_last_status() reports what happened.
+ * calling process; tflows_last_status() reports what happened.  Ab and the
+ * buffer part x(-NB:-1) are read only while a subdomain halo is registered
+ * (tflows_set_halo); otherwise the calls are the reference's one-domain run.
  *
  * Every call is synchronous and returns after x and r1 are back in host
  * memory.  The library keeps a per-device context (stream, workspace and a
