@@ -180,6 +180,8 @@ unsigned blocks_for(int n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
 // ---- registration ---------------------------------------------------------------------
 
+struct HaloSolve;
+
 struct HaloState {
     std::mutex mu;
     int npro = 0;
@@ -188,10 +190,11 @@ struct HaloState {
     tflows_exchange_fn exchange = nullptr;
     tflows_glosum_fn glosum = nullptr;
     void* user = nullptr;
+    HaloSolve* work = nullptr;  // buffers kept between calls (grow-only)
 };
 HaloState& state() {
-    static HaloState s;
-    return s;
+    static HaloState* s = new HaloState();  // outlives every caller, as par_mod does
+    return *s;
 }
 
 template <typename T>
@@ -212,25 +215,63 @@ struct DevBuf {
     }
 };
 
-// One solve's device arrays and the halo lists for its N.
+// The device arrays of the coupled solves and the halo lists of the current
+// call.  One instance lives in the halo state and is reused by every call
+// until the halo is cleared: buffers only grow, and the IC(0) pattern of the
+// last prec-2 call stays on the device while the caller passes the same
+// arrays (same addresses, sizes and sampled content hash as the legacy
+// topology cache).
 struct HaloSolve {
     const HaloState& h;
-    cudaStream_t s;
+    cudaStream_t s = nullptr;
     int n = 0, nb = 0, nnz = 0;
     DevBuf<int> acol, arow, adia, hrows, hptr, hkk, pkk, psrc;
     DevBuf<double> a, ab, d, phi, part, scal;
     DevBuf<double> vec[12];
     int nhrows = 0, npack = 0;
     double* phi_h = nullptr;
+    size_t phi_cap = 0;
     double* scal_h = nullptr;
     tflows_topology* topo = nullptr;
+    int topo_n = 0, topo_nnz = 0;
+    const int *topo_acol = nullptr, *topo_arow = nullptr, *topo_adia = nullptr;
+    unsigned long long topo_hash = 0;
     std::string msg;
 
-    HaloSolve(const HaloState& hs, cudaStream_t st) : h(hs), s(st) {}
+    explicit HaloSolve(const HaloState& hs) : h(hs) {}
     ~HaloSolve() {
         if (phi_h) cudaFreeHost(phi_h);
         if (scal_h) cudaFreeHost(scal_h);
         if (topo) tflows_topology_destroy(topo);
+    }
+    void begin(cudaStream_t st, int rows, int nbuf) {
+        s = st;
+        n = rows;
+        nb = nbuf;
+        msg.clear();
+    }
+
+    // The IC(0) pattern for these arrays, rebuilt only when they changed.
+    int ic_topology(const int* Acol, const int* Arow, const int* Adia) {
+        const unsigned long long hsh = legacy_pattern_hash(n, nnz, Acol, Arow, Adia);
+        if (topo && topo_n == n && topo_nnz == nnz && topo_acol == Acol && topo_arow == Arow &&
+            topo_adia == Adia && topo_hash == hsh)
+            return TFLOWS_OK;
+        if (topo) tflows_topology_destroy(topo);
+        topo = nullptr;
+        const int st = tflows_topology_create(&topo, n, nnz, Acol, Arow, Adia, 1, 0);
+        if (st != TFLOWS_OK) {
+            topo = nullptr;
+            msg = std::string("halo: IC(0) pattern: ") + tflows_last_error();
+            return st;
+        }
+        topo_n = n;
+        topo_nnz = nnz;
+        topo_acol = Acol;
+        topo_arow = Arow;
+        topo_adia = Adia;
+        topo_hash = hsh;
+        return TFLOWS_OK;
     }
 
     // Halo lists for this N: rows with their buffer cells in the reference's
@@ -309,8 +350,14 @@ struct HaloSolve {
         if (e == cudaSuccess) e = phi.need((size_t)nb);
         if (e == cudaSuccess) e = part.need(kDotBlocks);
         if (e == cudaSuccess) e = scal.need(1);
-        if (e == cudaSuccess && nb) e = cudaMallocHost(&phi_h, (size_t)nb * sizeof(double));
-        if (e == cudaSuccess) e = cudaMallocHost(&scal_h, sizeof(double));
+        if (e == cudaSuccess && (size_t)nb > phi_cap) {
+            if (phi_h) cudaFreeHost(phi_h);
+            phi_h = nullptr;
+            phi_cap = 0;
+            if ((e = cudaMallocHost(&phi_h, (size_t)nb * sizeof(double))) == cudaSuccess)
+                phi_cap = (size_t)nb;
+        }
+        if (e == cudaSuccess && !scal_h) e = cudaMallocHost(&scal_h, sizeof(double));
         if (e != cudaSuccess) return cuda(e, "halo workspace");
         e = cudaMemcpyAsync(acol.p, Acol, ((size_t)n + 1) * sizeof(int), cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess && nnz)
@@ -389,6 +436,13 @@ struct HaloSolve {
 
 }  // namespace
 
+void halo_release() {
+    HaloState& h = state();
+    std::lock_guard<std::mutex> lk(h.mu);
+    delete h.work;
+    h.work = nullptr;
+}
+
 bool halo_registered() {
     HaloState& h = state();
     std::lock_guard<std::mutex> lk(h.mu);
@@ -409,9 +463,9 @@ int halo_solve(int method, int n, int nb, int nonz, const double* A, const int* 
         rep.message = "halo: the transposed BiCG extension has no halo form";
         return rep.status = TFLOWS_UNSUPPORTED;
     }
-    HaloSolve hs(h, s);
-    hs.n = n;
-    hs.nb = nb;
+    if (!h.work) h.work = new HaloSolve(h);
+    HaloSolve& hs = *h.work;
+    hs.begin(s, n, nb);
     int st = hs.upload(A, Acol, Arow, Adia, Ab, nonz);
     if (st == TFLOWS_OK) st = hs.build_lists();
     const bool cgs = method == TFLOWS_METHOD_CGS;
@@ -421,10 +475,7 @@ int halo_solve(int method, int n, int nb, int nonz, const double* A, const int* 
         if (cudaError_t e = hs.d.need((size_t)n); e != cudaSuccess) st = hs.cuda(e, "D");
         else k_diag<<<blocks_for(n), kThreads, 0, s>>>(n, hs.adia.p, hs.a.p, hs.d.p);
     }
-    if (st == TFLOWS_OK && prec == 2) {
-        st = tflows_topology_create(&hs.topo, n, nonz - 1, Acol, Arow, Adia, 1, 0);
-        if (st != TFLOWS_OK) hs.msg = std::string("halo: IC(0) pattern: ") + tflows_last_error();
-    }
+    if (st == TFLOWS_OK && prec == 2) st = hs.ic_topology(Acol, Arow, Adia);
     if (st != TFLOWS_OK) {
         rep.message = hs.msg;
         return rep.status = st;
@@ -588,9 +639,9 @@ int halo_resid(int n, int nb, int nonz, const double* A, const int* Acol, const 
         msg = "halo: the NB of Resid differs from the registered NB";
         return TFLOWS_BAD_INPUT;
     }
-    HaloSolve hs(h, s);
-    hs.n = n;
-    hs.nb = nb;
+    if (!h.work) h.work = new HaloSolve(h);
+    HaloSolve& hs = *h.work;
+    hs.begin(s, n, nb);
     int st = hs.upload(A, Acol, Arow, nullptr, Ab, nonz);
     if (st == TFLOWS_OK) st = hs.build_lists();
     for (int v = 0; v < 2 && st == TFLOWS_OK; ++v)
@@ -631,6 +682,8 @@ int tflows_set_halo(int Npro, int NB, const int* NBBs, const int* NBBe, const in
     HaloState& h = state();
     std::lock_guard<std::mutex> lk(h.mu);
     if (Npro <= 0) {
+        delete h.work;  // frees the device and pinned buffers
+        h.work = nullptr;
         h.npro = 0;
         h.nb = 0;
         h.nbbs.clear();

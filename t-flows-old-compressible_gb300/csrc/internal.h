@@ -175,12 +175,17 @@ cudaError_t run_pattern_outer(const DeviceTopology& t, const double* lambda, con
 
 // Records the status and message tflows_last_status / tflows_last_error report.
 int report_status(int status, const std::string& msg);
+// The legacy topology cache's key hash of a 1-based pattern (about 8k
+// samples per array; every element with TFLOWS_TOPOLOGY_CHECK=full).
+unsigned long long legacy_pattern_hash(int n, int nnz, const int* Acol, const int* Arow,
+                                       const int* Adia);
 // Host-time phase mark of a legacy call run with TFLOWS_TRACE_LEGACY set.
 void trace_mark(const char* what);
 
 // Subdomain-coupled solves (halo.cu): whether a halo is registered, the
 // coupled solve of the Fortran-facing entry points and the coupled Resid.
 bool halo_registered();
+void halo_release();  // frees the coupled solves' buffers, keeps the registration
 int halo_solve(int method, int n, int nb, int nonz, const double* A, const int* Acol,
                const int* Arow, const int* Adia, const double* Ab, double* x, double* r1,
                int prec, int* niter, double tol, double* IniRes, double* FinRes,

@@ -609,6 +609,11 @@ int solve_on(tflows_topology* tp, const SolveRequest& rq0, const double* d_val, 
 
 }  // namespace
 
+unsigned long long tflows::legacy_pattern_hash(int n, int nnz, const int* Acol, const int* Arow,
+                                               const int* Adia) {
+    return pattern_hash(n, nnz, Acol, Arow, Adia);
+}
+
 // Status and message of the last call on this thread, for the other units.
 int tflows::report_status(int status, const std::string& msg) {
     t_status = status;
@@ -695,6 +700,7 @@ void tflows_forget_topologies(void) {
 }
 
 void tflows_finalize(void) {
+    halo_release();
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     for (auto& tp : c.cache) destroy_topo(tp.get());

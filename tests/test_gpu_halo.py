@@ -40,6 +40,11 @@ def _rank_solve(rank, world, kind, method, prec):
     try:
         out = tflows.solve_ex(method, sd.N, sd.NB, sd.NONZ, sd.A, sd.Acol, sd.Arow, sd.Adia,
                               sd.Ab, x, r, prec, 5000, tol)
+        # a second call reuses the kept buffers (and IC pattern): same answer
+        x2, r2 = x_in.copy(), sd.b.copy()
+        out2 = tflows.solve_ex(method, sd.N, sd.NB, sd.NONZ, sd.A, sd.Acol, sd.Arow, sd.Adia,
+                               sd.Ab, x2, r2, prec, 5000, tol)
+        assert out2.niter == out.niter and np.array_equal(x2, x) and np.array_equal(r2, r)
     finally:
         tflows.clear_halo()
     with oracle.halo(sd.Npro, sd.NB, sd.NBBs, sd.NBBe, sd.BufInd, exchange(sd), glosum()):
