@@ -516,6 +516,35 @@ def cfg4_cpu_estimate(pkg, dev, systems, topos, vals, bs, iters=2):
             "iterations_fp64": its}
 
 
+def spmv_block(topo, s, val, peak, dev, repeat=20):
+    """The standalone product y = A x on the workload's own system, FP64
+    (reference-arithmetic sums) and FP32 (difference form), SELL-32 slices
+    with one-byte column patterns when the mesh has few stencils.
+    Algorithmic bytes per product: the values and column data once, the
+    slice offsets, x read once and y written once.  Time per product from
+    CUDA events over `repeat` back-to-back products after one untimed call;
+    the matrix is several times larger than L2, so it streams from HBM every
+    product."""
+    import torch
+    x = torch.rand(s.N, dtype=torch.float64, device=dev)
+    y = torch.empty_like(x)
+    slices = (s.N + 31) // 32
+    cols_per = s.N if topo.patterns else None  # one byte per row with patterns
+    out = {"workload": f"{s.name}: y = A x", "n": s.N, "nnz": s.nnz,
+           "column_patterns": topo.patterns}
+    ref = s.scipy() @ x.cpu().numpy()
+    for label, fp32, sv in (("fp64", False, 8), ("fp32", True, 4)):
+        topo.spmv(val, x, y, repeat=1, fp32=fp32)
+        err = float(abs(y.cpu().numpy() - ref).max() / abs(ref).max())
+        sec = topo.spmv(val, x, y, repeat=repeat, fp32=fp32)
+        cols = cols_per if cols_per is not None else 4 * s.nnz
+        byts = sv * s.nnz + cols + 8 * (slices + 1) + 2 * s.N * sv
+        out[label] = {"us_per_product": 1e6 * sec, "algorithmic_bytes": byts,
+                      "gbs": byts / sec / 1e9, "frac": byts / sec / 1e9 / peak,
+                      "max_rel_diff_vs_host_product": err}
+    return out
+
+
 def legacy_e2e(pkg, s, method, prec, opts_kw, steps, warmup):
     """Seconds of `steps` calls of the Fortran-facing C ABI (tflows_cg /
     _bicg / _cgs) with A, x and b in pinned host memory and the given
@@ -994,10 +1023,12 @@ def main():
                     help="skip the config-1/2/5, SIMPLE-step and assembly blocks")
     ap.add_argument("--no-autotune", action="store_true",
                     help="fixed launch shape (256 threads, one slice per warp)")
-    ap.add_argument("--block", default=None, choices=["calcps", "newuvw", "cfg1", "cfg2", "ic"],
+    ap.add_argument("--block", default=None,
+                    choices=["calcps", "newuvw", "cfg1", "cfg2", "ic", "spmv"],
                     help="run only this block (an assembly on a --scale^3 box, default 128, "
-                         "the config-1 latency block, the config-2 block, or IC(0) CG on the "
-                         "config-3 system at --scale^3), print its JSON and exit")
+                         "the config-1 latency block, the config-2 block, IC(0) CG on the "
+                         "config-3 system at --scale^3, or the standalone product on the "
+                         "config-3 system at --scale^3, default 256), print its JSON and exit")
     ap.add_argument("--ic-iters", type=int, default=0,
                     help="--block ic: iteration cap of each solve (0 = to the tolerance)")
     ap.add_argument("--ic-tiled", type=int, default=-1,
@@ -1024,6 +1055,13 @@ def main():
             return
         if args.block == "cfg2":
             print(json.dumps(cfg2_block(pkg, dev, load_peaks()[0])), flush=True)
+            return
+        if args.block == "spmv":
+            s = make_workload(pkg, "cfg3", args.scale)
+            topo = pkg.Topology.from_system(s)
+            val = torch.from_numpy(s.A[:-1].copy()).to(dev)
+            print(json.dumps(spmv_block(topo, s, val, load_peaks()[0], dev)), flush=True)
+            topo.close()
             return
         if args.block == "ic":
             tiled = (0, 1) if args.ic_tiled < 0 else (args.ic_tiled,)
@@ -1140,6 +1178,8 @@ def main():
         line["comparison"] = cfg3_comparison(pkg, dev, topo, s, val, b, headline, x.clone())
         line["rel_err_vs_tight_fp64"] = line["comparison"]["mixed_ic_exact_bf16"]["rel_err_vs_tight_fp64"]
         line["speedups"] = line["comparison"]["speedups"]
+    if rank == 0 and not args.no_extras:
+        line["spmv"] = spmv_block(topo, s, val, peak, dev)
     topo.close()
     del val, b, x
     torch.cuda.empty_cache()
