@@ -477,6 +477,16 @@ def batched_cfg4(pkg, dev, reps, count=48, autotune=True):
     return out
 
 
+def lpt_makespan(times, cores):
+    """Wall time of independent jobs run one per core, longest first, each
+    on the core that frees up first."""
+    loads = [0.0] * max(1, cores)
+    for t in sorted(times, reverse=True):
+        k = loads.index(min(loads))
+        loads[k] += t
+    return max(loads)
+
+
 def cfg4_cpu_estimate(pkg, dev, systems, topos, vals, bs, iters=2):
     """The oracle on the batch, one solve per host core.  Each system's
     oracle solve is its set-up (an oracle run with no iterations) plus
@@ -504,11 +514,8 @@ def cfg4_cpu_estimate(pkg, dev, systems, topos, vals, bs, iters=2):
         its.append(r["iterations"])
         est.append((t1 - t0) + r["iterations"] * t_it)
     cores = os.cpu_count() or 1
-    loads = [0.0] * cores
-    for t in sorted(est, reverse=True):
-        k = loads.index(min(loads))
-        loads[k] += t
-    return {"seconds_per_batch": max(loads), "systems_per_s": len(est) / max(loads),
+    span = lpt_makespan(est, cores)
+    return {"seconds_per_batch": span, "systems_per_s": len(est) / span,
             "one_core_seconds": sum(est), "cores": cores, "kind": "port",
             "sample": f"per system the oracle's set-up and {iters} whole iterations, scaled to the "
                       "iteration count of the reference-arithmetic GPU solve at 1e-8 relative; "

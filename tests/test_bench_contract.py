@@ -25,3 +25,14 @@ def test_reference_arm_prints_one_json_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
     assert "workload" in line["config"]
+
+
+def test_batch_cpu_schedule_longest_first():
+    """The batched CPU baseline places solves longest first on the least
+    loaded core: its wall time is the busiest core's total."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.lpt_makespan([5.0, 4.0, 3.0, 3.0, 3.0], 2) == 10.0
+    assert bench.lpt_makespan([1.0] * 6, 3) == 2.0
+    assert bench.lpt_makespan([7.0, 1.0], 16) == 7.0
+    assert bench.lpt_makespan([], 4) == 0.0
